@@ -1,0 +1,535 @@
+// Hand-written sm_103a kernels of the GKR prove path (M31).
+//
+// Data layout in HBM: every per-copy table is row-major rows x N u32 (row r, copy k at
+// r*N + k), the byte layout of a proof vector (VectorizedM31::to_bytes, M31.hpp:420-426),
+// so a warp's 16-byte loads along a row are fully coalesced.  Scalar tables that do not
+// depend on the copy (eq tables, gate weights, the phase-two h(y) factor) are plain
+// arrays of u32 read by broadcast.
+//
+// Reference counterparts:
+//   k_evaluate     CircuitLayer::evaluate                     include/circuit/circuit.hpp:92-105
+//   k_eq           _eq_evals_at                               include/LinearGKR/sumcheck_common.hpp:17-53
+//   k_weights      the scalar factors of _prepare_g_x_vals    include/LinearGKR/sumcheck_helper.hpp:188-229
+//   k_hg_round0    _prepare_g_x_vals + poly_eval_at(0)        sumcheck_helper.hpp:172-231, 68-102
+//   k_round        receive_challenge + poly_eval_at(k)        sumcheck_helper.hpp:104-133, 68-102
+//   k_s_build      _prepare_h_y_vals (copy-independent part)  sumcheck_helper.hpp:233-261
+//   k_wsum         eval_multilinear via an eq table           include/poly_commit/poly.hpp:88-104
+#include "kernels.cuh"
+#include "m31.cuh"
+
+namespace gkrgpu {
+
+const char* const kKernelNames[K_NUM_KERNELS] = {"check_canonical", "evaluate", "eq_table", "gate_weights",
+                                                 "hg_build_round0", "round_fold_lane", "round_fold_scalar",
+                                                 "phase2_s_build", "weighted_row_sum"};
+
+namespace {
+
+using m31::add;
+using m31::fold;
+using m31::mul;
+using m31::sub;
+
+__device__ __forceinline__ uint4 ld4(const uint32_t* __restrict__ base, uint64_t row, uint32_t N, uint32_t lane0) {
+    return __ldg(reinterpret_cast<const uint4*>(base + row * N + lane0));
+}
+__device__ __forceinline__ void st4(uint32_t* base, uint64_t row, uint32_t N, uint32_t lane0, uint4 v) {
+    *reinterpret_cast<uint4*>(base + row * N + lane0) = v;
+}
+__device__ __forceinline__ uint32_t comp(const uint4& v, int l) { return l == 0 ? v.x : l == 1 ? v.y : l == 2 ? v.z : v.w; }
+__device__ __forceinline__ uint4 mk4(const uint32_t (&a)[4]) { return make_uint4(a[0], a[1], a[2], a[3]); }
+
+// Canonical residue of a sum of many canonical values (< 2^64 total).
+__device__ __forceinline__ uint32_t reduce64(unsigned long long x) {
+    x = (x & m31::P) + (x >> 31);
+    x = (x & m31::P) + (x >> 31);
+    uint32_t s = (uint32_t)x;
+    return m31::umin(s, s - m31::P);
+}
+
+// Block reduction of C components x 4 lanes per thread over the CTA's row slices, one
+// 64-bit atomic add per (component, lane) into red.acc, then the last CTA to arrive
+// turns the totals into canonical values, hands them to fin(lane, vals[C]) and re-zeroes
+// the scratch for the next launch.
+template <int C, class Fin>
+__device__ __forceinline__ void reduce_epilogue(const uint32_t (&acc)[C][4], const Geo& g, bool active, RedScratch red,
+                                                Fin fin) {
+    extern __shared__ uint32_t smem[];
+    const uint32_t tid = threadIdx.x, B = blockDim.x;
+#pragma unroll
+    for (int c = 0; c < C; c++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) smem[(c * 4 + l) * B + tid] = active ? acc[c][l] : 0u;
+    __syncthreads();
+    const uint32_t tpr = g.tpr, rps = g.rps;
+    for (uint32_t o = tid; o < (uint32_t)C * 4 * tpr; o += B) {
+        const uint32_t cl = o / tpr, q = o - cl * tpr;
+        const uint32_t* col = smem + cl * B + q;
+        unsigned long long s = 0;
+        for (uint32_t r = 0; r < rps; r++) s += col[r * tpr];
+        const uint32_t c = cl >> 2, l = cl & 3;
+        const uint32_t lane = (blockIdx.y * tpr + q) * 4 + l;
+        atomicAdd(&red.acc[(size_t)c * g.N + lane], s);
+    }
+    __threadfence();
+    __syncthreads();
+    __shared__ unsigned int is_last;
+    if (tid == 0) is_last = (atomicAdd(red.ticket, 1u) == gridDim.x * gridDim.y - 1) ? 1u : 0u;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    for (uint32_t lane = tid; lane < g.N; lane += B) {
+        uint32_t v[C];
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            unsigned long long* p = &red.acc[(size_t)c * g.N + lane];
+            v[c] = reduce64(__ldcg(p));
+            *p = 0ull;
+        }
+        fin(lane, v);
+    }
+    if (tid == 0) *red.ticket = 0u;
+}
+
+struct TileIdx {
+    uint32_t q, rs, lane0;
+    bool active;
+};
+__device__ __forceinline__ TileIdx tile_idx(const Geo& g) {
+    TileIdx t;
+    t.q = threadIdx.x % g.tpr;
+    t.rs = threadIdx.x / g.tpr;
+    t.lane0 = (blockIdx.y * g.tpr + t.q) * 4;
+    t.active = t.rs < g.rps;
+    return t;
+}
+
+// ---------------------------------------------------------------- input check
+__global__ void k_check_canonical(const uint32_t* __restrict__ v, uint64_t n, unsigned int* flag) {
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    unsigned int bad = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n / 4; i += stride) {
+        uint4 x = __ldg(reinterpret_cast<const uint4*>(v) + i);
+        bad |= (x.x >= m31::P) | (x.y >= m31::P) | (x.z >= m31::P) | (x.w >= m31::P);
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+}
+
+// ---------------------------------------------------------------- layer evaluation
+// out[o] = sum over mul gates (o, i0, i1, c) of in[i0]*in[i1]*c + sum over add gates
+// (o, i0, c) of in[i0]*c, gates grouped by o (CSR), so every output row is written once.
+__global__ void __launch_bounds__(256) k_evaluate(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint64_t O,
+                                                  const uint32_t* __restrict__ mo_off, const uint4* __restrict__ mo_g,
+                                                  const uint32_t* __restrict__ ao_off, const uint2* __restrict__ ao_g,
+                                                  Geo g) {
+    const TileIdx t = tile_idx(g);
+    if (!t.active) return;
+    for (uint64_t o = (uint64_t)blockIdx.x * g.rps + t.rs; o < O; o += (uint64_t)gridDim.x * g.rps) {
+        uint32_t acc[4] = {0u, 0u, 0u, 0u};
+        const uint32_t m0 = __ldg(mo_off + o), m1 = __ldg(mo_off + o + 1);
+        for (uint32_t k = m0; k < m1; k++) {
+            const uint4 gt = __ldg(mo_g + k);
+            const uint4 a = ld4(in, gt.x, g.N, t.lane0), b = ld4(in, gt.y, g.N, t.lane0);
+#pragma unroll
+            for (int l = 0; l < 4; l++) acc[l] = add(acc[l], mul(mul(comp(a, l), comp(b, l)), gt.z));
+        }
+        const uint32_t a0 = __ldg(ao_off + o), a1 = __ldg(ao_off + o + 1);
+        for (uint32_t k = a0; k < a1; k++) {
+            const uint2 gt = __ldg(ao_g + k);
+            const uint4 a = ld4(in, gt.x, g.N, t.lane0);
+#pragma unroll
+            for (int l = 0; l < 4; l++) acc[l] = add(acc[l], mul(comp(a, l), gt.y));
+        }
+        st4(out, o, g.N, t.lane0, mk4(acc));
+    }
+}
+
+// ---------------------------------------------------------------- eq tables
+// out[j][z] = f1 * eq(r1_j, z) + f2 * eq(r2_j, z), bit t of z paired with r[t]
+// (little-endian, sumcheck_common.hpp:17-53); eq(r, 0) = 1 - r, eq(r, 1) = r.
+__global__ void k_eq(uint32_t* __restrict__ out, EqArgs a) {
+    const uint64_t size = 1ull << a.nvars;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t z = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; z < size; z += stride) {
+        for (uint32_t j = 0; j < a.reps; j++) {
+            uint32_t e1 = a.f1, e2 = a.f2;
+            for (uint32_t t = 0; t < a.nvars; t++) {
+                const bool bit = (z >> t) & 1;
+                e1 = mul(e1, bit ? a.r1[j][t] : sub(1u, a.r1[j][t]));
+                if (a.f2) e2 = mul(e2, bit ? a.r2[j][t] : sub(1u, a.r2[j][t]));
+            }
+            out[(uint64_t)j * size + z] = add(e1, a.f2 ? e2 : 0u);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- phase-one scalar factors
+// w[k].j = c_k * eqc_j[z_k] for every mul gate k (gates in CSR-by-x order) and
+// a[x].j = sum over add gates (z, x, c) of c * eqc_j[z]: the copy-independent parts of
+// hg(x) = sum_mul v(y) c eqc(z) + sum_add c eqc(z) (sumcheck_helper.hpp:203-229).
+__global__ void k_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* __restrict__ eqc,
+                          const uint4* __restrict__ mx_g, const uint32_t* __restrict__ ax_off,
+                          const uint2* __restrict__ ax_g, uint4* __restrict__ a_out, uint4* __restrict__ w_out,
+                          uint32_t reps) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t n = I > Gm ? I : Gm;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (i < Gm) {
+            const uint4 gt = __ldg(mx_g + i);  // (y, z, c, 0)
+            uint32_t w[3] = {0u, 0u, 0u};
+            for (uint32_t j = 0; j < reps; j++) w[j] = mul(gt.z, __ldg(eqc + (uint64_t)j * O + gt.y));
+            w_out[i] = make_uint4(w[0], w[1], w[2], 0u);
+        }
+        if (i < I) {
+            uint32_t s[3] = {0u, 0u, 0u};
+            const uint32_t k0 = __ldg(ax_off + i), k1 = __ldg(ax_off + i + 1);
+            for (uint32_t k = k0; k < k1; k++) {
+                const uint2 gt = __ldg(ax_g + k);  // (z, c)
+                for (uint32_t j = 0; j < reps; j++) s[j] = add(s[j], mul(gt.y, __ldg(eqc + (uint64_t)j * O + gt.x)));
+            }
+            a_out[i] = make_uint4(s[0], s[1], s[2], 0u);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- round finishers
+template <int R>
+struct RoundFin {
+    uint32_t* out;       // R x 3 x N: evaluations at 0, 1, 2 per repetition
+    const uint32_t* vx;  // R x N phase-two factor v(rx), or null
+    uint32_t N;
+    __device__ void operator()(uint32_t lane, const uint32_t* v) const {
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            uint32_t p0 = v[3 * j], p1 = v[3 * j + 1];
+            uint32_t p2 = m31::eval_at_two(p0, p1, v[3 * j + 2]);
+            if (vx) {
+                const uint32_t x = vx[(size_t)j * N + lane];
+                p0 = mul(p0, x); p1 = mul(p1, x); p2 = mul(p2, x);
+            }
+            out[(size_t)(3 * j) * N + lane] = p0;
+            out[(size_t)(3 * j + 1) * N + lane] = p1;
+            out[(size_t)(3 * j + 2) * N + lane] = p2;
+        }
+    }
+};
+
+template <int R>
+struct CopyFin {
+    uint32_t* out;  // R x N
+    uint32_t N;
+    __device__ void operator()(uint32_t lane, const uint32_t* v) const {
+#pragma unroll
+        for (int j = 0; j < R; j++) out[(size_t)j * N + lane] = v[j];
+    }
+};
+
+template <int R>
+__device__ __forceinline__ void accum_pair(uint32_t (&acc)[3 * R][4], int j, const uint32_t (&f0)[4],
+                                           const uint32_t (&f1)[4], const uint32_t (&h0)[4], const uint32_t (&h1)[4]) {
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+        acc[3 * j][l] = add(acc[3 * j][l], mul(f0[l], h0[l]));
+        acc[3 * j + 1][l] = add(acc[3 * j + 1][l], mul(f1[l], h1[l]));
+        acc[3 * j + 2][l] = add(acc[3 * j + 2][l], mul(add(f0[l], f1[l]), add(h0[l], h1[l])));
+    }
+}
+
+// ---------------------------------------------------------------- phase one: hg build + round 0
+// For each pair (x0, x1) = (2i, 2i+1): hg_j[x] = a_j[x] + sum over mul gates (x, y, k) of
+// v[y] * w_j[k], written for the later folds, then the round-0 sums of v(x) hg_j(x).
+template <int R>
+__global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ v, uint64_t I,
+                                                   const uint32_t* __restrict__ mx_off, const uint4* __restrict__ mx_g,
+                                                   const uint4* __restrict__ a4, const uint4* __restrict__ w4,
+                                                   uint32_t* hg0, uint32_t* hg1, uint32_t* hg2, Geo g, RedScratch red,
+                                                   uint32_t* evals_out) {
+    const TileIdx t = tile_idx(g);
+    uint32_t acc[3 * R][4];
+#pragma unroll
+    for (int c = 0; c < 3 * R; c++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[c][l] = 0u;
+    uint32_t* hg[3] = {hg0, hg1, hg2};
+    if (t.active) {
+        const uint64_t npairs = I >> 1;
+        for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
+            uint32_t h[2][R][4];
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                const uint64_t x = 2 * i + s;
+                const uint4 a = __ldg(a4 + x);
+#pragma unroll
+                for (int j = 0; j < R; j++)
+#pragma unroll
+                    for (int l = 0; l < 4; l++) h[s][j][l] = comp(a, j);
+                const uint32_t k0 = __ldg(mx_off + x), k1 = __ldg(mx_off + x + 1);
+                for (uint32_t k = k0; k < k1; k++) {
+                    const uint32_t y = __ldg(&mx_g[k].x);
+                    const uint4 w = __ldg(w4 + k);
+                    const uint4 vy = ld4(v, y, g.N, t.lane0);
+#pragma unroll
+                    for (int j = 0; j < R; j++)
+#pragma unroll
+                        for (int l = 0; l < 4; l++) h[s][j][l] = add(h[s][j][l], mul(comp(vy, l), comp(w, j)));
+                }
+#pragma unroll
+                for (int j = 0; j < R; j++) st4(hg[j], x, g.N, t.lane0, mk4(h[s][j]));
+            }
+            const uint4 v0 = ld4(v, 2 * i, g.N, t.lane0), v1 = ld4(v, 2 * i + 1, g.N, t.lane0);
+            const uint32_t f0[4] = {v0.x, v0.y, v0.z, v0.w}, f1[4] = {v1.x, v1.y, v1.z, v1.w};
+#pragma unroll
+            for (int j = 0; j < R; j++) accum_pair<R>(acc, j, f0, f1, h[0][j], h[1][j]);
+        }
+    }
+    reduce_epilogue<3 * R>(acc, g, t.active, red, RoundFin<R>{evals_out, nullptr, g.N});
+}
+
+// ---------------------------------------------------------------- fold + reduce round
+// FOLD: the inputs hold 4*npairs rows; rows (4i, 4i+1) and (4i+2, 4i+3) are folded at the
+// previous round's challenge r_j into rows 2i and 2i+1 of the outputs, which are stored
+// for the next round and summed into this round's evaluations.  Without FOLD the inputs
+// hold 2*npairs rows and are summed directly (first round of phase two).
+// SHARED: every repetition folds the same source table (the layer input at round 1).
+// LANE_HG: hg is a per-copy table (phase one); otherwise it is a copy-independent scalar
+// table s_j (phase two) and the finisher multiplies the sums by vx_j.
+template <int R, bool SHARED, bool LANE_HG, bool FOLD>
+__global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx, Geo g,
+                                               RedScratch red, uint32_t* evals_out) {
+    const TileIdx t = tile_idx(g);
+    uint32_t acc[3 * R][4];
+#pragma unroll
+    for (int c = 0; c < 3 * R; c++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[c][l] = 0u;
+    if (t.active) {
+        for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
+            uint4 sh[4];
+            if (SHARED) {
+                if (FOLD) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) sh[k] = ld4(p.fsrc[0], 4 * i + k, g.N, t.lane0);
+                } else {
+                    sh[0] = ld4(p.fsrc[0], 2 * i, g.N, t.lane0);
+                    sh[1] = ld4(p.fsrc[0], 2 * i + 1, g.N, t.lane0);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                uint32_t f0[4], f1[4], h0[4], h1[4];
+                const uint32_t r = p.r[j];
+                if (FOLD) {
+                    uint4 a[4];
+#pragma unroll
+                    for (int k = 0; k < 4; k++) a[k] = SHARED ? sh[k] : ld4(p.fsrc[j], 4 * i + k, g.N, t.lane0);
+#pragma unroll
+                    for (int l = 0; l < 4; l++) {
+                        f0[l] = fold(comp(a[0], l), comp(a[1], l), r);
+                        f1[l] = fold(comp(a[2], l), comp(a[3], l), r);
+                    }
+                    st4(p.fdst[j], 2 * i, g.N, t.lane0, mk4(f0));
+                    st4(p.fdst[j], 2 * i + 1, g.N, t.lane0, mk4(f1));
+                } else {
+                    const uint4 a0 = SHARED ? sh[0] : ld4(p.fsrc[j], 2 * i, g.N, t.lane0);
+                    const uint4 a1 = SHARED ? sh[1] : ld4(p.fsrc[j], 2 * i + 1, g.N, t.lane0);
+#pragma unroll
+                    for (int l = 0; l < 4; l++) { f0[l] = comp(a0, l); f1[l] = comp(a1, l); }
+                }
+                if (LANE_HG) {
+                    if (FOLD) {
+                        uint4 b[4];
+#pragma unroll
+                        for (int k = 0; k < 4; k++) b[k] = ld4(p.hsrc[j], 4 * i + k, g.N, t.lane0);
+#pragma unroll
+                        for (int l = 0; l < 4; l++) {
+                            h0[l] = fold(comp(b[0], l), comp(b[1], l), r);
+                            h1[l] = fold(comp(b[2], l), comp(b[3], l), r);
+                        }
+                        st4(p.hdst[j], 2 * i, g.N, t.lane0, mk4(h0));
+                        st4(p.hdst[j], 2 * i + 1, g.N, t.lane0, mk4(h1));
+                    } else {
+                        const uint4 b0 = ld4(p.hsrc[j], 2 * i, g.N, t.lane0), b1 = ld4(p.hsrc[j], 2 * i + 1, g.N, t.lane0);
+#pragma unroll
+                        for (int l = 0; l < 4; l++) { h0[l] = comp(b0, l); h1[l] = comp(b1, l); }
+                    }
+                } else {
+                    uint32_t s0, s1;
+                    if (FOLD) {
+                        const uint4 s = __ldg(reinterpret_cast<const uint4*>(p.hsrc[j]) + i);
+                        s0 = fold(s.x, s.y, r);
+                        s1 = fold(s.z, s.w, r);
+                        if (t.q == 0 && blockIdx.y == 0)
+                            *reinterpret_cast<uint2*>(p.hdst[j] + 2 * i) = make_uint2(s0, s1);
+                    } else {
+                        const uint2 s = __ldg(reinterpret_cast<const uint2*>(p.hsrc[j]) + i);
+                        s0 = s.x;
+                        s1 = s.y;
+                    }
+#pragma unroll
+                    for (int l = 0; l < 4; l++) { h0[l] = s0; h1[l] = s1; }
+                }
+                accum_pair<R>(acc, j, f0, f1, h0, h1);
+            }
+        }
+    }
+    reduce_epilogue<3 * R>(acc, g, t.active, red, RoundFin<R>{evals_out, LANE_HG ? nullptr : vx, g.N});
+}
+
+// ---------------------------------------------------------------- phase two: s(y)
+// s_j[y] = sum over mul gates (z, x, y, c) of eqc_j[z] * eq_rx_j[x] * c: the
+// copy-independent factor of h(y) = v(rx) s(y) (sumcheck_helper.hpp:250-259).
+__global__ void k_s_build(uint64_t I, uint64_t O, const uint32_t* __restrict__ my_off, const uint4* __restrict__ my_g,
+                          const uint32_t* __restrict__ eqc, const uint32_t* __restrict__ eqrx, uint32_t* __restrict__ s_out,
+                          uint64_t s_stride, uint32_t reps) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t y = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; y < I; y += stride) {
+        uint32_t s[3] = {0u, 0u, 0u};
+        const uint32_t k0 = __ldg(my_off + y), k1 = __ldg(my_off + y + 1);
+        for (uint32_t k = k0; k < k1; k++) {
+            const uint4 gt = __ldg(my_g + k);  // (x, z, c, 0)
+            for (uint32_t j = 0; j < reps; j++) {
+                const uint32_t e = mul(__ldg(eqc + (uint64_t)j * O + gt.y), __ldg(eqrx + (uint64_t)j * I + gt.x));
+                s[j] = add(s[j], mul(e, gt.z));
+            }
+        }
+        for (uint32_t j = 0; j < reps; j++) s_out[(uint64_t)j * s_stride + y] = s[j];
+    }
+}
+
+// ---------------------------------------------------------------- weighted row sums
+// out[j] = sum_z eq_j[z] * vals[z]: eval_multilinear at r_j for each repetition.
+template <int R>
+__global__ void __launch_bounds__(256) k_wsum(const uint32_t* __restrict__ vals, uint64_t rows,
+                                              const uint32_t* __restrict__ eq, Geo g, RedScratch red,
+                                              uint32_t* out) {
+    const TileIdx t = tile_idx(g);
+    uint32_t acc[R][4];
+#pragma unroll
+    for (int c = 0; c < R; c++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[c][l] = 0u;
+    if (t.active) {
+        for (uint64_t z = (uint64_t)blockIdx.x * g.rps + t.rs; z < rows; z += (uint64_t)gridDim.x * g.rps) {
+            const uint4 v = ld4(vals, z, g.N, t.lane0);
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                const uint32_t w = __ldg(eq + (uint64_t)j * rows + z);
+#pragma unroll
+                for (int l = 0; l < 4; l++) acc[j][l] = add(acc[j][l], mul(comp(v, l), w));
+            }
+        }
+    }
+    reduce_epilogue<R>(acc, g, t.active, red, CopyFin<R>{out, g.N});
+}
+
+uint32_t grid_1d(uint64_t n, uint32_t block) {
+    uint64_t b = (n + block - 1) / block;
+    if (b < 1) b = 1;
+    if (b > 152ull * 16) b = 152ull * 16;
+    return (uint32_t)b;
+}
+
+}  // namespace
+
+LaunchShape row_shape(const Geo& g, uint64_t rows, uint32_t block, uint32_t ctas_cap, uint32_t smem_components) {
+    LaunchShape s;
+    const uint32_t groups = g.N / (4 * g.tpr);
+    uint64_t need = (rows + g.rps - 1) / g.rps;
+    uint64_t cap = ctas_cap / groups;
+    if (cap < 1) cap = 1;
+    if (need < 1) need = 1;
+    s.grid = dim3((uint32_t)(need < cap ? need : cap), groups, 1);
+    s.block = dim3(block, 1, 1);
+    s.smem = (size_t)smem_components * 4 * block * sizeof(uint32_t);
+    return s;
+}
+
+cudaError_t launch_check_canonical(const uint32_t* v, uint64_t n, unsigned int* flag, cudaStream_t s) {
+    k_check_canonical<<<grid_1d(n / 4, 256), 256, 0, s>>>(v, n, flag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_evaluate(const uint32_t* in, uint32_t* out, uint64_t O, const uint32_t* mo_off, const uint4* mo_g,
+                            const uint32_t* ao_off, const uint2* ao_g, const Geo& g, uint32_t block, uint32_t ctas,
+                            cudaStream_t s) {
+    LaunchShape sh = row_shape(g, O, block, ctas, 0);
+    k_evaluate<<<sh.grid, sh.block, 0, s>>>(in, out, O, mo_off, mo_g, ao_off, ao_g, g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_eq(uint32_t* out, const EqArgs& a, cudaStream_t s) {
+    k_eq<<<grid_1d(1ull << a.nvars, 256), 256, 0, s>>>(out, a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* eqc, const uint4* mx_g,
+                           const uint32_t* ax_off, const uint2* ax_g, uint4* a_out, uint4* w_out, uint32_t reps,
+                           cudaStream_t s) {
+    k_weights<<<grid_1d(I > Gm ? I : Gm, 256), 256, 0, s>>>(I, Gm, O, eqc, mx_g, ax_off, ax_g, a_out, w_out, reps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint32_t* mx_off, const uint4* mx_g,
+                             const uint4* a4, const uint4* w4, uint32_t* const hg[3], const Geo& g, uint32_t block,
+                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
+    LaunchShape sh = row_shape(g, I / 2, block, ctas, 3 * reps);
+    switch (reps) {
+        case 1: k_hg_round0<1><<<sh.grid, sh.block, sh.smem, s>>>(v, I, mx_off, mx_g, a4, w4, hg[0], hg[1], hg[2], g, red, evals_out); break;
+        case 2: k_hg_round0<2><<<sh.grid, sh.block, sh.smem, s>>>(v, I, mx_off, mx_g, a4, w4, hg[0], hg[1], hg[2], g, red, evals_out); break;
+        case 3: k_hg_round0<3><<<sh.grid, sh.block, sh.smem, s>>>(v, I, mx_off, mx_g, a4, w4, hg[0], hg[1], hg[2], g, red, evals_out); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <int R>
+static void round_dispatch(bool shared_src, bool lane_hg, bool fold_, const LaunchShape& sh, cudaStream_t s,
+                           const RoundPtrs& p, uint64_t npairs, const uint32_t* vx, const Geo& g, RedScratch red,
+                           uint32_t* ev) {
+#define GKR_ROUND(SH, LH, FO) k_round<R, SH, LH, FO><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, ev)
+    if (lane_hg) {
+        if (shared_src) GKR_ROUND(true, true, true);
+        else GKR_ROUND(false, true, true);
+    } else if (fold_) {
+        if (shared_src) GKR_ROUND(true, false, true);
+        else GKR_ROUND(false, false, true);
+    } else {
+        GKR_ROUND(true, false, false);
+    }
+#undef GKR_ROUND
+}
+
+cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, const RoundPtrs& p, uint64_t npairs,
+                         const uint32_t* vx, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
+                         uint32_t* evals_out, cudaStream_t s) {
+    if (lane_hg && !fold_) return cudaErrorInvalidValue;  // phase-one round 0 lives in k_hg_round0
+    if (!fold_ && !shared_src) return cudaErrorInvalidValue;
+    LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
+    switch (reps) {
+        case 1: round_dispatch<1>(shared_src, lane_hg, fold_, sh, s, p, npairs, vx, g, red, evals_out); break;
+        case 2: round_dispatch<2>(shared_src, lane_hg, fold_, sh, s, p, npairs, vx, g, red, evals_out); break;
+        case 3: round_dispatch<3>(shared_src, lane_hg, fold_, sh, s, p, npairs, vx, g, red, evals_out); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_s_build(uint64_t I, uint64_t O, const uint32_t* my_off, const uint4* my_g, const uint32_t* eqc,
+                           const uint32_t* eqrx, uint32_t* s_out, uint64_t s_stride, uint32_t reps, cudaStream_t s) {
+    k_s_build<<<grid_1d(I, 256), 256, 0, s>>>(I, O, my_off, my_g, eqc, eqrx, s_out, s_stride, reps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wsum(int reps, const uint32_t* vals, uint64_t rows, const uint32_t* eq, const Geo& g,
+                        uint32_t block, uint32_t ctas, RedScratch red, uint32_t* out, cudaStream_t s) {
+    LaunchShape sh = row_shape(g, rows, block, ctas, reps);
+    switch (reps) {
+        case 1: k_wsum<1><<<sh.grid, sh.block, sh.smem, s>>>(vals, rows, eq, g, red, out); break;
+        case 2: k_wsum<2><<<sh.grid, sh.block, sh.smem, s>>>(vals, rows, eq, g, red, out); break;
+        case 3: k_wsum<3><<<sh.grid, sh.block, sh.smem, s>>>(vals, rows, eq, g, red, out); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace gkrgpu

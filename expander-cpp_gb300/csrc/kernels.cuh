@@ -1,0 +1,84 @@
+// Device kernels of the GKR prove path and their host-side launch wrappers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gkrgpu {
+
+// Thread tile for a table of rows x N lanes stored row-major (row r, lane k at r*N + k).
+// Each thread owns 4 consecutive lanes (one 16-byte load); tpr threads cover a slice of
+// 4*tpr lanes of one row, rps such slices (rows) share a CTA, and gridDim.y = N/(4*tpr)
+// lane groups cover the whole row.
+struct Geo {
+    uint32_t N;    // lanes (data-parallel circuit copies), multiple of 4
+    uint32_t tpr;  // threads per row slice
+    uint32_t rps;  // row slices per CTA (blockDim.x / tpr)
+};
+
+// Scratch of the reducing kernels: per-(component, lane) 64-bit accumulators and the
+// arrival ticket of the last-CTA finisher.  Both are left zeroed by every launch.
+struct RedScratch {
+    unsigned long long* acc;  // components x N
+    unsigned int* ticket;
+};
+
+struct EqArgs {
+    uint32_t r1[3][32];
+    uint32_t r2[3][32];
+    uint32_t f1, f2;  // factors alpha (table 1) and beta (table 2; 0 = no second table)
+    uint32_t nvars;
+    uint32_t reps;
+};
+
+struct RoundPtrs {
+    const uint32_t* fsrc[3];
+    uint32_t* fdst[3];
+    const uint32_t* hsrc[3];
+    uint32_t* hdst[3];
+    uint32_t r[3];
+};
+
+struct LaunchShape {
+    dim3 grid, block;
+    size_t smem;
+};
+
+// Kernel identifiers for launch accounting.
+enum KernelId {
+    K_CHECK = 0,
+    K_EVALUATE,
+    K_EQ,
+    K_WEIGHTS,
+    K_HG_ROUND0,
+    K_ROUND_LANE,
+    K_ROUND_SCALAR,
+    K_S_BUILD,
+    K_WSUM,
+    K_NUM_KERNELS
+};
+extern const char* const kKernelNames[K_NUM_KERNELS];
+
+// Shape of a row-tiled launch over `rows` rows; ctas_cap bounds gridDim.x * gridDim.y.
+LaunchShape row_shape(const Geo& g, uint64_t rows, uint32_t block, uint32_t ctas_cap, uint32_t smem_components);
+
+// Launch wrappers (all asynchronous on `s`).
+cudaError_t launch_check_canonical(const uint32_t* v, uint64_t n, unsigned int* flag, cudaStream_t s);
+cudaError_t launch_evaluate(const uint32_t* in, uint32_t* out, uint64_t O, const uint32_t* mo_off, const uint4* mo_g,
+                            const uint32_t* ao_off, const uint2* ao_g, const Geo& g, uint32_t block, uint32_t ctas,
+                            cudaStream_t s);
+cudaError_t launch_eq(uint32_t* out, const EqArgs& a, cudaStream_t s);
+cudaError_t launch_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* eqc, const uint4* mx_g,
+                           const uint32_t* ax_off, const uint2* ax_g, uint4* a_out, uint4* w_out, uint32_t reps,
+                           cudaStream_t s);
+cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint32_t* mx_off, const uint4* mx_g,
+                             const uint4* a4, const uint4* w4, uint32_t* const hg[3], const Geo& g, uint32_t block,
+                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
+cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold, const RoundPtrs& p, uint64_t npairs,
+                         const uint32_t* vx, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
+                         uint32_t* evals_out, cudaStream_t s);
+cudaError_t launch_s_build(uint64_t I, uint64_t O, const uint32_t* my_off, const uint4* my_g, const uint32_t* eqc,
+                           const uint32_t* eqrx, uint32_t* s_out, uint64_t s_stride, uint32_t reps, cudaStream_t s);
+cudaError_t launch_wsum(int reps, const uint32_t* vals, uint64_t rows, const uint32_t* eq, const Geo& g,
+                        uint32_t block, uint32_t ctas, RedScratch red, uint32_t* out, cudaStream_t s);
+
+}  // namespace gkrgpu

@@ -1,0 +1,198 @@
+"""Python mirror of the reference prover API on top of the C ABI.
+
+Reference (PolyhedraZK/Expander-cpp)                       here
+  Config (include/configuration/config.hpp:26-86)        Config
+  Prover(config).prepare_mem(circuit); prove(circuit)    Prover(config).prepare_mem(circuit); prove(circuit)
+    (include/LinearGKR/LinearGKR.hpp:34-91)                -> (claimed_v (R, N) uint32, Proof)
+  Circuit::evaluate (include/circuit/circuit.hpp:273-280) Context.evaluate / Prover.evaluate
+  Proof (include/fiat_shamir/transcript.hpp:13-85)       Proof (bytes + write/read of the length-prefixed file)
+
+The circuit input (the reference's layers[0].input_layer_vals) is a (2^n, N) uint32 array
+set with Circuit.set_input or passed to prove() directly.
+"""
+import ctypes
+import struct
+
+import numpy as np
+
+from . import _lib
+from .circuit import Circuit
+
+
+class Config:
+    """Config of the reference: 100-bit security, RAW commitment, M31, SHA-256 transcript."""
+
+    def __init__(self, grinding_bits: int = 10):
+        self.security_bits = 100
+        self.grinding_bits = int(grinding_bits)
+        self.field_size = 31
+        self.PC_type = "Raw"
+        self.field_type = "M31"
+        self.FS_hash = "SHA256"
+
+    def get_num_repetitions(self) -> int:
+        return _lib.load().gkrgpu_num_repetitions(self.grinding_bits)
+
+
+class Proof:
+    """Proof bytes (the transcript).  write/read use the reference's file format: a 4-byte
+    little-endian length then the bytes (transcript.hpp:54-84)."""
+
+    def __init__(self, data: bytes = b""):
+        self.bytes = bytes(data)
+
+    def __len__(self):
+        return len(self.bytes)
+
+    def __eq__(self, other):
+        return isinstance(other, Proof) and self.bytes == other.bytes
+
+    def write(self, path):
+        with open(path, "wb") as f:
+            f.write(struct.pack("<I", len(self.bytes) & 0xFFFFFFFF))
+            f.write(self.bytes)
+
+    @staticmethod
+    def read(path):
+        with open(path, "rb") as f:
+            (n,) = struct.unpack("<I", f.read(4))
+            return Proof(f.read(n))
+
+
+class DeviceCircuit:
+    """A circuit's wiring resident on the device (gkrgpu_circuit_load)."""
+
+    def __init__(self, ctx: "Context", circuit: Circuit):
+        lib = _lib.load()
+        circuit.validate()
+        self.ctx = ctx
+        self.n_layers = len(circuit.layers)
+        self.log_input_size = circuit.log_input_size
+        self.nb_output_vars = circuit.layers[-1].nb_output_vars
+        descs = (_lib.LayerDesc * self.n_layers)()
+        keep = []
+        for k, l in enumerate(circuit.layers):
+            m = np.ascontiguousarray(l.mul, dtype=np.uint32)
+            a = np.ascontiguousarray(l.add, dtype=np.uint32)
+            keep += [m, a]
+            descs[k] = _lib.LayerDesc(l.nb_output_vars, l.nb_input_vars, m.shape[0], a.shape[0],
+                                      m.ctypes.data if m.size else None, a.ctypes.data if a.size else None)
+        h = ctypes.c_void_p()
+        _lib.check(lib.gkrgpu_circuit_load(ctx.handle, descs, self.n_layers, ctypes.byref(h)))
+        self.handle = h
+
+    def proof_size(self, n_copies, grinding_bits=10):
+        return _lib.load().gkrgpu_proof_size(self.handle, n_copies, grinding_bits)
+
+    def free(self):
+        if getattr(self, "handle", None):
+            _lib.load().gkrgpu_circuit_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    """One CUDA device, its stream and the reusable prover workspace (gkrgpu_create)."""
+
+    def __init__(self, device: int = 0):
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(lib.gkrgpu_create(device, ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().gkrgpu_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load(self, circuit: Circuit) -> DeviceCircuit:
+        return DeviceCircuit(self, circuit)
+
+    def evaluate(self, dc: DeviceCircuit, witness, all_layers=False):
+        """Circuit::evaluate on the device; returns the output rows, or with all_layers every
+        layer's input rows followed by the output rows, as one (rows, N) array."""
+        lib = _lib.load()
+        w = np.ascontiguousarray(witness, dtype=np.uint32)
+        rows = lib.gkrgpu_value_rows(dc.handle, int(all_layers))
+        out = np.empty((rows, w.shape[1]), np.uint32)
+        _lib.check(lib.gkrgpu_evaluate(self.handle, dc.handle, w.shape[1], w.ctypes.data, out.ctypes.data,
+                                       int(all_layers)))
+        return out
+
+    def prove(self, dc: DeviceCircuit, witness, grinding_bits=10, out=None):
+        """Prover::prove; returns (claimed_v (R, N) uint32, proof bytes).  `out` may be a
+        preallocated uint8 buffer of at least proof_size bytes (e.g. pinned host memory)."""
+        lib = _lib.load()
+        w = np.ascontiguousarray(witness, dtype=np.uint32)
+        N = w.shape[1]
+        cap = dc.proof_size(N, grinding_bits)
+        buf = np.empty(cap, np.uint8) if out is None else out
+        R = lib.gkrgpu_num_repetitions(grinding_bits)
+        cv = np.empty((R, N), np.uint32)
+        plen = ctypes.c_uint64()
+        _lib.check(lib.gkrgpu_prove(self.handle, dc.handle, N, grinding_bits, w.ctypes.data, buf.ctypes.data,
+                                    buf.nbytes, ctypes.byref(plen), cv.ctypes.data))
+        return cv, (buf[:plen.value].tobytes() if out is None else plen.value)
+
+    def prove_device(self, dc: DeviceCircuit, d_input: int, n_copies: int, out_buf, grinding_bits=10):
+        """Prover::prove with the input already in device memory at address d_input."""
+        lib = _lib.load()
+        R = lib.gkrgpu_num_repetitions(grinding_bits)
+        cv = np.empty((R, n_copies), np.uint32)
+        plen = ctypes.c_uint64()
+        _lib.check(lib.gkrgpu_prove_device(self.handle, dc.handle, n_copies, grinding_bits, ctypes.c_void_p(d_input),
+                                           out_buf.ctypes.data, out_buf.nbytes, ctypes.byref(plen), cv.ctypes.data))
+        return cv, plen.value
+
+    def set_timing(self, enabled: bool):
+        _lib.check(_lib.load().gkrgpu_set_timing(self.handle, int(enabled)))
+
+    def reset_stats(self):
+        _lib.check(_lib.load().gkrgpu_reset_stats(self.handle))
+
+    def kernel_stats(self):
+        lib = _lib.load()
+        arr = (_lib.KernelStat * 32)()
+        n = lib.gkrgpu_kernel_stats(self.handle, arr, 32)
+        return {arr[i].name.decode(): {"launches": arr[i].launches, "ms": arr[i].total_ms,
+                                       "bytes": arr[i].algorithmic_bytes} for i in range(min(n, 32))}
+
+    def set_tile(self, threads_per_row=0, block=0, ctas=0):
+        _lib.check(_lib.load().gkrgpu_set_tile(self.handle, threads_per_row, block, ctas))
+
+
+class Prover:
+    """gkr::Prover (include/LinearGKR/LinearGKR.hpp:34-91) on the GPU."""
+
+    def __init__(self, config: Config = None, ctx: Context = None):
+        self.config = config or Config()
+        self.ctx = ctx or Context(0)
+        self._dc = None
+        self._circuit = None
+
+    def prepare_mem(self, circuit: Circuit):
+        """Uploads the circuit's wiring (the reference allocates its scratch pads here)."""
+        if self._circuit is not circuit:
+            self._dc = self.ctx.load(circuit)
+            self._circuit = circuit
+
+    def prove(self, circuit: Circuit, witness=None):
+        if self._circuit is not circuit:
+            self.prepare_mem(circuit)
+        w = circuit.input_values if witness is None else witness
+        if w is None:
+            raise ValueError("no circuit input: call circuit.set_input(values) or pass witness")
+        cv, proof = self.ctx.prove(self._dc, w, self.config.grinding_bits)
+        return cv, Proof(proof)

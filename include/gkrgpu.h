@@ -1,0 +1,130 @@
+/* gkrgpu: GB300-native GKR prover for data-parallel layered circuits over M31.
+ *
+ * C ABI of the drop-in boundary.  Each entry point replaces one piece of the reference
+ * prove path of PolyhedraZK/Expander-cpp (file:line below are paths in that project).
+ * Plain pointers and sizes only; every call returns a status code (GKRGPU_OK = 0) and
+ * the message of the last failure on the calling thread is gkrgpu_last_error().
+ * No C++ exception crosses this boundary.  Device waits inside the library are bounded.
+ *
+ * Value layout: a table of R rows for N data-parallel circuit copies is R*N uint32
+ * values, row-major (row i, copy k at i*N + k), each canonical in [0, 2^31 - 1).  One row
+ * is the byte image of the reference's vector field element (VectorizedM31::to_bytes,
+ * include/field/M31.hpp:420-426) for N copies.
+ */
+#ifndef GKRGPU_H
+#define GKRGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GKRGPU_OK 0
+#define GKRGPU_ERR_INVALID 1   /* bad argument (shape, id out of range, non-canonical value) */
+#define GKRGPU_ERR_CUDA 2      /* CUDA runtime failure */
+#define GKRGPU_ERR_NOMEM 3     /* device or pinned host allocation failed */
+#define GKRGPU_ERR_CAPACITY 4  /* caller buffer too small (required size still reported) */
+#define GKRGPU_ERR_TIMEOUT 5   /* a bounded wait expired */
+#define GKRGPU_ERR_STATE 6     /* object used in the wrong state */
+
+typedef struct gkrgpu_ctx gkrgpu_ctx;
+typedef struct gkrgpu_circuit gkrgpu_circuit;
+
+/* Gate<M31,2> and Gate<M31,1>, include/circuit/circuit.hpp:13-30 (16 and 12 bytes). */
+typedef struct { uint32_t o_id, i0, i1, coef; } gkrgpu_mul_gate;
+typedef struct { uint32_t o_id, i0, coef; } gkrgpu_add_gate;
+
+/* CircuitLayer, include/circuit/circuit.hpp:68-116.  nb_output_vars of layer l must equal
+ * nb_input_vars of layer l+1; layer 0 reads the circuit input. */
+typedef struct {
+    uint32_t nb_output_vars, nb_input_vars;
+    uint64_t n_mul, n_add;
+    const gkrgpu_mul_gate* mul;
+    const gkrgpu_add_gate* add;
+} gkrgpu_layer_desc;
+
+/* Per-kernel launch accounting (see gkrgpu_kernel_stats). */
+typedef struct {
+    const char* name;
+    uint64_t launches;
+    double total_ms;          /* CUDA-event time, only while timing is enabled */
+    double algorithmic_bytes; /* compulsory HBM bytes summed over the launches */
+} gkrgpu_kernel_stat;
+
+/* Message of the last failure on this thread ("" if none). */
+const char* gkrgpu_last_error(void);
+
+/* Library version string. */
+const char* gkrgpu_version(void);
+
+/* Config::get_num_repetitions for M31 with 100-bit security,
+ * include/configuration/config.hpp:61-65 (3 for the default grinding_bits = 10). */
+int gkrgpu_num_repetitions(int grinding_bits);
+
+/* A context owns one CUDA device, a stream and a reusable device workspace.
+ * Replaces the reference's per-prover scratch (GKRScratchPad,
+ * include/LinearGKR/scratch_pad.hpp:8-65; Prover::prepare_mem, LinearGKR.hpp:49-56). */
+int gkrgpu_create(int device, gkrgpu_ctx** out);
+void gkrgpu_destroy(gkrgpu_ctx* ctx);
+
+/* Uploads a circuit's wiring (the gate lists of every layer) to the device and builds
+ * the per-layer gate indexes the kernels use.  Replaces building Circuit<F,F_primitive>
+ * (include/circuit/circuit.hpp:118-251).  Ids and coefficients are checked. */
+int gkrgpu_circuit_load(gkrgpu_ctx* ctx, const gkrgpu_layer_desc* layers, int n_layers, gkrgpu_circuit** out);
+void gkrgpu_circuit_free(gkrgpu_circuit* circuit);
+
+/* Proof bytes of Prover::prove for this circuit: RAW commitment (2^nb_input_vars(0) rows
+ * of 4N bytes) + 32 grinding bytes + per layer R*(6*nb_input_vars + 2) rows of 4N bytes. */
+uint64_t gkrgpu_proof_size(const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits);
+
+/* Rows of the value tables gkrgpu_evaluate writes with all_layers = 1. */
+uint64_t gkrgpu_value_rows(const gkrgpu_circuit* circuit, int all_layers);
+
+/* Circuit::evaluate (include/circuit/circuit.hpp:92-105,273-280) on the device.
+ * input: host table of 2^nb_input_vars(0) rows.  out: host table of the last layer's
+ * output rows (all_layers = 0) or of every layer's input rows followed by the output
+ * rows (all_layers = 1). */
+int gkrgpu_evaluate(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, const uint32_t* input,
+                    uint32_t* out, int all_layers);
+
+/* Prover::prove (include/LinearGKR/LinearGKR.hpp:58-90): RAW commitment, grinding,
+ * gkr_prove (include/LinearGKR/gkr.hpp:24-73) and the empty RAW openings, after
+ * Circuit::evaluate.  input: host table (2^nb_input_vars(0) rows, n_copies lanes, a
+ * multiple of 4).  proof_out receives the transcript bytes (proof_len set even when the
+ * capacity is short); claimed_v receives R rows of n_copies lanes (gkr.hpp:52-55).
+ * The bytes are identical to the reference prover's for the same circuit and input. */
+int gkrgpu_prove(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
+                 const uint32_t* input, uint8_t* proof_out, uint64_t proof_cap, uint64_t* proof_len,
+                 uint32_t* claimed_v);
+
+/* As gkrgpu_prove with the input table already resident in device memory (d_input, on
+ * this context's device).  The commitment bytes are read back from the device. */
+int gkrgpu_prove_device(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
+                        const uint32_t* d_input, uint8_t* proof_out, uint64_t proof_cap, uint64_t* proof_len,
+                        uint32_t* claimed_v);
+
+/* Device / pinned host buffers for callers without a CUDA allocator of their own. */
+int gkrgpu_device_alloc(gkrgpu_ctx* ctx, uint64_t bytes, void** out);
+int gkrgpu_device_free(gkrgpu_ctx* ctx, void* p);
+int gkrgpu_host_alloc(uint64_t bytes, void** out);
+int gkrgpu_host_free(void* p);
+int gkrgpu_memcpy_h2d(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t bytes);
+int gkrgpu_memcpy_d2h(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t bytes);
+
+/* Launch accounting.  With timing on, every kernel launch is bracketed by CUDA events on
+ * the context's stream.  gkrgpu_kernel_stats fills up to cap entries (one per kernel
+ * kind) and returns how many kinds exist; gkrgpu_reset_stats clears the counters. */
+int gkrgpu_set_timing(gkrgpu_ctx* ctx, int enabled);
+int gkrgpu_reset_stats(gkrgpu_ctx* ctx);
+int gkrgpu_kernel_stats(gkrgpu_ctx* ctx, gkrgpu_kernel_stat* out, int cap);
+
+/* Tuning of the row tile: threads per row slice (each covers 4 copies), CTA size and the
+ * CTA budget of the reducing kernels.  0 keeps the current value. */
+int gkrgpu_set_tile(gkrgpu_ctx* ctx, uint32_t threads_per_row, uint32_t block, uint32_t ctas);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

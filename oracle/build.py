@@ -1,0 +1,51 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+``build_oracle()`` compiles the C restatement into ``oracle/build/libgkr_oracle.so``
+with plain ``gcc -O3`` (portable: no -march flags, builds on x86-64 and aarch64).
+``build_ref()`` runs ``oracle/build_ref.sh`` when the reference tree exists.
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "build")
+ORACLE_SO = os.path.join(BUILD, "libgkr_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libgkr_ref.so")
+REFERENCE_ROOT = "/root/reference"
+
+
+def _stale(target, sources):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def build_oracle(force=False):
+    srcs = [os.path.join(HERE, "gkr_oracle.c"), os.path.join(HERE, "gkr_oracle.h")]
+    if not force and not _stale(ORACLE_SO, srcs):
+        return ORACLE_SO
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = ORACLE_SO + ".tmp"
+    subprocess.check_call(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-pthread", "-Wall",
+                           srcs[0], "-o", tmp])
+    os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+def build_ref(force=False):
+    """Compile the reference driver (x86-64 only, needs the reference tree)."""
+    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "include", "LinearGKR")):
+        return None
+    if os.uname().machine != "x86_64":
+        return None
+    srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "build_ref.sh")]
+    if not force and not _stale(REF_SO, srcs):
+        return REF_SO
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT])
+    return REF_SO
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    print(build_ref(force=True))
