@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 GKR prover on the large plain workload.
+
+Workload (one step = one complete Prover::prove: RAW commitment, grinding, Circuit::evaluate
+and the GKR sumcheck of every layer): a seeded synthetic M31 circuit of 24 layers whose
+widths alternate 2^18 / 2^20 gates, 60% fan-in-2 mul / 40% fan-in-2 add, wiring local to
+2^12-gate windows with probability 0.8, 1024 data-parallel copies, uniform witness,
+SHA-256 transcript, RAW commitment.  The witness (1 GiB) and the per-layer tables
+(~90 GiB) are far larger than L2, so no flush is needed between steps.
+
+  value : proofs/s with the input already resident in HBM (gkrgpu_prove_device)
+  e2e   : proofs/s through the C ABI with host buffers (gkrgpu_prove: input H2D, proof
+          and claims D2H inside every step)
+  roofline: the kernel with the largest device time; achieved = its algorithmic bytes per
+          launch / its CUDA-event time per launch, against the measured HBM copy peak.
+  cpu_baseline: the CPU oracle port (oracle/gkr_oracle.c) on this host's cores, one proof
+          per thread, on the same circuit at 8 copies, scaled to 1024-copy proofs/s.
+
+--impl reference runs the CPU prover alone (the compiled reference where it was built on
+this machine, else the oracle port) and prints the same JSON line with "impl".
+Multi-GPU (torchrun): independent replicas, one per rank, no data-path collective.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "expander-cpp_gb300")]
+
+import numpy as np  # noqa: E402
+
+METRIC = "GKR proofs/s batched vs plain on 1 GB300 (byte-identical proofs); p99; HBM GB/s"
+UNIT = "proofs/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--copies", type=int, default=1024)
+    ap.add_argument("--layers", type=int, default=24)
+    ap.add_argument("--narrow", type=int, default=18)
+    ap.add_argument("--wide", type=int, default=20)
+    ap.add_argument("--cpu-copies", type=int, default=8, help="copies per proof in the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- distributed plumbing
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=5)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- workload
+def workload(args):
+    from gkr_gb300 import circuit as gc
+    widths = [args.narrow if l % 2 == 0 else args.wide for l in range(args.layers + 1)]
+    circ = gc.random_circuit(2024, widths, p_mul=0.6, p_local=0.8, window=1 << 12)
+    cfg = {"workload": f"{args.layers} layers alternating 2^{args.narrow}/2^{args.wide} gates, 60% mul / 40% add "
+                       f"fan-in-2, wiring local to 2^12-gate windows w.p. 0.8, {args.copies} copies, uniform M31 "
+                       "witness, SHA-256 transcript, RAW commitment (one plain proof per step)",
+           "n_copies": args.copies, "layers": args.layers, "widths_log2": [args.narrow, args.wide],
+           "mul_gates": circ.nb_mul_gates, "add_gates": circ.nb_add_gates, "grinding_bits": 10, "repetitions": 3,
+           "l2": "inputs and tables larger than L2 (no flush needed)", "field": "M31"}
+    return circ, widths, cfg
+
+
+def cpu_sample(circ, args, n_steps=1, warmup=0):
+    """Times the CPU prover (all host cores, one proof per thread) on the workload's circuit at
+    args.cpu_copies copies; returns (1024-copy-equivalent proofs/s per step, info)."""
+    from gkr_gb300 import circuit as gc
+    from oracle.oracle import Oracle, Reference
+    threads = len(os.sched_getaffinity(0))
+    w = gc.random_witness(7, circ.log_input_size, args.cpu_copies)
+    use_ref = Reference.available()
+    if use_ref:
+        ref = Reference()
+
+        def run():
+            t0 = time.perf_counter()
+            ths = [threading.Thread(target=ref.prove, args=(circ, w), kwargs={"native": args.cpu_copies == 8})
+                   for _ in range(threads)]
+            for t in ths:
+                t.start()
+            for t in ths:
+                t.join()
+            return time.perf_counter() - t0
+        kind = "reference"
+    else:
+        orc = Oracle()
+
+        def run():
+            return orc.bench(circ, w, threads, 1)
+        kind = "port"
+    for _ in range(warmup):
+        run()
+    vals = []
+    for _ in range(n_steps):
+        dt = run()
+        vals.append(threads / dt * args.cpu_copies / args.copies)
+    info = {"cores": threads, "kind": kind,
+            "sample": f"{threads} threads x 1 proof of the same circuit at {args.cpu_copies} copies "
+                      f"(evaluate + prove), scaled by {args.cpu_copies}/{args.copies} to {args.copies}-copy proofs/s"}
+    return vals, info
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- arms
+def run_reference(args, D):
+    if D.rank != 0:
+        return
+    circ, widths, cfg = workload(args)
+    vals, info = cpu_sample(circ, args, n_steps=args.steps, warmup=args.warmup)
+    v = statistics.mean(vals)
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic", "config": cfg, "impl": "reference",
+            "cpu_baseline": dict(info, value=v, unit=UNIT),
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, D):
+    from gkr_gb300 import circuit as gc
+    from gkr_gb300.prover import Context, DeviceBuffer, HostBuffer
+
+    device = D.local_rank
+    circ, widths, cfg = workload(args)
+    N = args.copies
+    ctx = Context(device)
+    dc = ctx.load(circ)
+    rows = 1 << circ.log_input_size
+    plen = dc.proof_size(N)
+    hin = HostBuffer(rows * N * 4, np.uint32)
+    witness = hin.array.reshape(rows, N)
+    gc.random_witness(1000 + D.rank, circ.log_input_size, N, out=witness)
+    din = DeviceBuffer(ctx, rows * N * 4)
+    din.upload(witness)
+    pbuf = HostBuffer(plen)
+    proof = pbuf.array
+
+    # ---- value: input resident in HBM
+    for _ in range(args.warmup):
+        ctx.prove_device(dc, din.ptr, N, proof)
+    ctx.reset_stats()
+    ctx.set_timing(True)
+    clocks = ClockSampler(device)
+    clocks.start()
+    D.barrier()
+    ctx.mark(0)
+    for k in range(args.steps):
+        ctx.prove_device(dc, din.ptr, N, proof)
+        ctx.mark(k + 1)
+    total_ms = ctx.elapsed_ms(0, args.steps)
+    D.barrier()
+    clk = clocks.stop()
+    ctx.set_timing(False)
+    step_ms = [ctx.elapsed_ms(k, k + 1) for k in range(args.steps)]
+    stats = ctx.kernel_stats()
+    launches = int(sum(s["launches"] for s in stats.values()))
+    max_ms = D.max(total_ms)
+    value = D.world * args.steps / (max_ms / 1000.0)
+    ref_digest = bytes(proof[plen - 4096:plen])
+
+    # ---- e2e: host buffers through the C ABI
+    e2e = None
+    if not args.no_e2e:
+        ctx.prove(dc, witness, out=proof)
+        ctx.reset_stats()
+        D.barrier()
+        ctx.mark(0)
+        for k in range(args.steps):
+            ctx.prove(dc, witness, out=proof)
+            ctx.mark(k + 1)
+        e2e_ms = D.max(ctx.elapsed_ms(0, args.steps))
+        h2d, d2h = ctx.transfer_stats()
+        e2e = {"value": D.world * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
+               "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
+               "ms_per_step": e2e_ms / args.steps,
+               "note": "gkrgpu_prove from pinned host memory; commitment assembled on the host from the input"}
+        assert bytes(proof[plen - 4096:plen]) == ref_digest, "e2e proof differs from the device-input proof"
+
+    # ---- roofline of the dominant kernel
+    peak, peak_kind = peaks()
+    dom = max(stats.items(), key=lambda kv: kv[1]["ms"])
+    name, s = dom
+    per_launch_bytes = s["bytes"] / max(s["launches"], 1)
+    per_launch_ms = s["ms"] / max(s["launches"], 1)
+    achieved = per_launch_bytes / (per_launch_ms / 1000.0) / 1e9 if per_launch_ms > 0 else 0.0
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        ratio = json.load(open(tfile)).get(name, {}).get("traffic_over_algorithmic")
+        if ratio:
+            traffic = per_launch_bytes * ratio
+    roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": per_launch_bytes, "launches": s["launches"],
+                "ms_per_launch": per_launch_ms}
+    total_bytes = sum(v["bytes"] for v in stats.values()) / args.steps
+    kernel_ms = sum(v["ms"] for v in stats.values()) / args.steps
+    kernels = {k: {"launches_per_step": v["launches"] / args.steps, "ms_per_step": v["ms"] / args.steps,
+                   "GBps": (v["bytes"] / (v["ms"] / 1000.0) / 1e9) if v["ms"] else None}
+               for k, v in stats.items() if v["launches"]}
+
+    cpu = None
+    if D.rank == 0 and not args.no_cpu_baseline:
+        vals, info = cpu_sample(circ, args)
+        cpu = dict(info, value=vals[0], unit=UNIT)
+
+    if D.rank == 0:
+        p50 = statistics.median(step_ms)
+        p99 = float(np.percentile(step_ms, 99))
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": D.world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+                "config": dict(cfg, parallelism=f"replicas x{D.world}" if D.world > 1 else "single"),
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clk, "latency_ms": {"p50": p50, "p99": p99, "steps": step_ms},
+                "hbm": {"algorithmic_bytes_per_proof": total_bytes,
+                        "GBps_over_step": total_bytes / (max_ms / args.steps / 1000.0) / 1e9,
+                        "GBps_over_kernels": total_bytes / (kernel_ms / 1000.0) / 1e9,
+                        "kernel_ms_per_step": kernel_ms},
+                "kernels": kernels, "proof_bytes": plen}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    D = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, D)
+        else:
+            run_ours(args, D)
+    finally:
+        D.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -175,6 +175,8 @@ struct gkrgpu_ctx {
 
     // launch accounting
     bool timing = false;
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;
+    cudaEvent_t markers[64] = {};
     uint64_t launches[K_NUM_KERNELS] = {};
     double ms[K_NUM_KERNELS] = {};
     double bytes[K_NUM_KERNELS] = {};
@@ -199,6 +201,8 @@ struct gkrgpu_ctx {
         }
         sb[0].release(); sb[1].release();
         for (auto e : events) cudaEventDestroy(e);
+        for (auto e : markers)
+            if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -238,6 +242,12 @@ struct gkrgpu_ctx {
         ev_used = 0;
     }
     void sync() { ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
+    // Stream-ordered copy, counted in the transfer statistics.
+    void copy(void* dst, const void* src, size_t n, cudaMemcpyKind kind, const char* what) {
+        ck(cudaMemcpyAsync(dst, src, n, kind, stream), what);
+        if (kind == cudaMemcpyHostToDevice) h2d_bytes += n;
+        if (kind == cudaMemcpyDeviceToHost) d2h_bytes += n;
+    }
 
     Geo geo(uint32_t N) const {
         const uint32_t Q = N / 4;
@@ -443,7 +453,7 @@ struct Prover {
         ck(cudaMemsetAsync(c.flag.p, 0, 4, c.stream), "cudaMemsetAsync");
         const uint64_t n = C.in_rows(0) * N;
         c.launch(K_CHECK, (double)n * 4, [&] { return launch_check_canonical(vals[0], n, c.flag.as<unsigned>(), c.stream); });
-        ck(cudaMemcpyAsync(c.h_flag.p, c.flag.p, 4, cudaMemcpyDeviceToHost, c.stream), "cudaMemcpyAsync");
+        c.copy(c.h_flag.p, c.flag.p, 4, cudaMemcpyDeviceToHost, "input check readback");
     }
     void require_canonical() {
         if (*c.h_flag.as<unsigned>()) fail(GKRGPU_ERR_INVALID, "input contains a value >= 2^31 - 1");
@@ -465,12 +475,11 @@ struct Prover {
     // D2H of the 3R evaluation rows and optionally `rows_from` rows 0..1 for each repetition.
     void fetch(const uint32_t* const* rows_from, bool shared_rows) {
         const uint64_t rowb = (uint64_t)N * 4;
-        ck(cudaMemcpyAsync(c.h_evals.p, c.evals.p, 3ull * R * rowb, cudaMemcpyDeviceToHost, c.stream), "fetch evals");
+        c.copy(c.h_evals.p, c.evals.p, 3ull * R * rowb, cudaMemcpyDeviceToHost, "fetch evals");
         if (rows_from) {
             for (int j = 0; j < R; j++) {
                 const uint32_t* src = shared_rows ? rows_from[0] : rows_from[j];
-                ck(cudaMemcpyAsync(c.h_rows.as<char>() + 2 * j * rowb, src, 2 * rowb, cudaMemcpyDeviceToHost, c.stream),
-                   "fetch rows");
+                c.copy(c.h_rows.as<char>() + 2 * j * rowb, src, 2 * rowb, cudaMemcpyDeviceToHost, "fetch rows");
             }
         }
         c.sync();
@@ -575,7 +584,7 @@ struct Prover {
             return launch_s_build(I, O, Ly.my_off, Ly.my_g, c.eqc.as<uint32_t>(), c.eqrx.as<uint32_t>(),
                                   c.sb[0].as<uint32_t>(), sstride, R, c.stream);
         });
-        ck(cudaMemcpyAsync(c.vx.p, vxh, R * rowb, cudaMemcpyHostToDevice, c.stream), "vx upload");
+        c.copy(c.vx.p, vxh, R * rowb, cudaMemcpyHostToDevice, "vx upload");
         {
             RoundPtrs p;
             memset(&p, 0, sizeof(p));
@@ -624,7 +633,7 @@ struct Prover {
         reserve(d_input == nullptr);
         layout_values(d_input);
         if (h_input)
-            ck(cudaMemcpyAsync(vals[0], h_input, in_bytes, cudaMemcpyHostToDevice, c.stream), "input upload");
+            c.copy(vals[0], h_input, in_bytes, cudaMemcpyHostToDevice, "input upload");
         check_input();
         evaluate();
 
@@ -634,7 +643,7 @@ struct Prover {
         if (h_input) {
             t.append(h_input, in_bytes);
         } else {
-            ck(cudaMemcpyAsync(t.tail(), d_input, in_bytes, cudaMemcpyDeviceToHost, c.stream), "commitment readback");
+            c.copy(t.tail(), d_input, in_bytes, cudaMemcpyDeviceToHost, "commitment readback");
             c.sync();
             require_canonical();
             t.appended(in_bytes);
@@ -657,7 +666,7 @@ struct Prover {
             return launch_wsum(R, vals[L], OL, c.eqc.as<uint32_t>(), g, c.block, c.cta_budget(), c.red(),
                                c.cv.as<uint32_t>(), c.stream);
         });
-        ck(cudaMemcpyAsync(c.h_cv.p, c.cv.p, R * rowb, cudaMemcpyDeviceToHost, c.stream), "claims readback");
+        c.copy(c.h_cv.p, c.cv.p, R * rowb, cudaMemcpyDeviceToHost, "claims readback");
         c.sync();
         require_canonical();
         memcpy(claimed_v, c.h_cv.p, R * rowb);
@@ -681,7 +690,7 @@ struct Prover {
         const uint64_t rowb = (uint64_t)N * 4;
         reserve(true);
         layout_values(nullptr);
-        ck(cudaMemcpyAsync(vals[0], h_input, C.in_rows(0) * rowb, cudaMemcpyHostToDevice, c.stream), "input upload");
+        c.copy(vals[0], h_input, C.in_rows(0) * rowb, cudaMemcpyHostToDevice, "input upload");
         check_input();
         evaluate();
         c.sync();
@@ -914,6 +923,39 @@ int gkrgpu_reset_stats(gkrgpu_ctx* ctx) {
         }
         ctx->recs.clear();
         ctx->ev_used = 0;
+        ctx->h2d_bytes = ctx->d2h_bytes = 0;
+    });
+}
+
+int gkrgpu_mark(gkrgpu_ctx* ctx, int slot) {
+    return guarded([&] {
+        check_ctx(ctx);
+        if (slot < 0 || slot >= 64) fail(GKRGPU_ERR_INVALID, "marker slot must be in [0, 64)");
+        DeviceGuard dg(ctx->device);
+        if (!ctx->markers[slot]) ck(cudaEventCreate(&ctx->markers[slot]), "cudaEventCreate");
+        ck(cudaEventRecord(ctx->markers[slot], ctx->stream), "cudaEventRecord");
+    });
+}
+
+int gkrgpu_elapsed_ms(gkrgpu_ctx* ctx, int from_slot, int to_slot, double* ms) {
+    return guarded([&] {
+        check_ctx(ctx);
+        if (!ms || from_slot < 0 || from_slot >= 64 || to_slot < 0 || to_slot >= 64 || !ctx->markers[from_slot] ||
+            !ctx->markers[to_slot])
+            fail(GKRGPU_ERR_INVALID, "unrecorded marker slot");
+        DeviceGuard dg(ctx->device);
+        ck(cudaEventSynchronize(ctx->markers[to_slot]), "cudaEventSynchronize");
+        float t = 0.f;
+        ck(cudaEventElapsedTime(&t, ctx->markers[from_slot], ctx->markers[to_slot]), "cudaEventElapsedTime");
+        *ms = t;
+    });
+}
+
+int gkrgpu_transfer_stats(gkrgpu_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes) {
+    return guarded([&] {
+        check_ctx(ctx);
+        if (h2d_bytes) *h2d_bytes = ctx->h2d_bytes;
+        if (d2h_bytes) *d2h_bytes = ctx->d2h_bytes;
     });
 }
 

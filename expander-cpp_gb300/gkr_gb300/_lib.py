@@ -62,6 +62,9 @@ SIGNATURES = [
     ("gkrgpu_reset_stats", _I, [_P]),
     ("gkrgpu_kernel_stats", _I, [_P, _P, _I]),
     ("gkrgpu_set_tile", _I, [_P, _U32, _U32, _U32]),
+    ("gkrgpu_mark", _I, [_P, _I]),
+    ("gkrgpu_elapsed_ms", _I, [_P, _I, _I, ctypes.POINTER(ctypes.c_double)]),
+    ("gkrgpu_transfer_stats", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
 ]
 
 _lib = None

@@ -173,10 +173,20 @@ def random_circuit(seed, widths, p_mul=0.5, p_local=0.0, window=1 << 12):
     return Circuit([random_layer(st, widths[l + 1], widths[l], p_mul, p_local, window) for l in range(len(widths) - 1)])
 
 
-def random_witness(seed, nb_input_vars, n_copies):
-    """Uniform M31 witness, shape (2^nb_input_vars, n_copies), canonical."""
+def random_witness(seed, nb_input_vars, n_copies, out=None):
+    """Uniform M31 witness, shape (2^nb_input_vars, n_copies), canonical.  Generated in
+    chunks (so a 1 GiB witness does not need several GiB of temporaries); `out` may be a
+    preallocated uint32 array of that shape (e.g. pinned host memory)."""
+    rows = 1 << nb_input_vars
+    n = rows * n_copies
+    res = np.empty((rows, n_copies), np.uint32) if out is None else out
+    flat = res.reshape(-1)
     st = Stream(seed ^ 0x5EED5EED5EED5EED)
-    return st.field((1 << nb_input_vars) * n_copies).reshape(1 << nb_input_vars, n_copies)
+    chunk = 1 << 22
+    for s in range(0, n, chunk):
+        m = min(chunk, n - s)
+        flat[s:s + m] = st.field(m)
+    return res
 
 
 # ---------------------------------------------------------------- named workloads

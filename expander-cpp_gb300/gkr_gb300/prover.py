@@ -172,6 +172,67 @@ class Context:
     def set_tile(self, threads_per_row=0, block=0, ctas=0):
         _lib.check(_lib.load().gkrgpu_set_tile(self.handle, threads_per_row, block, ctas))
 
+    def mark(self, slot: int):
+        """Records timing marker `slot` on the context's stream."""
+        _lib.check(_lib.load().gkrgpu_mark(self.handle, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = ctypes.c_double()
+        _lib.check(_lib.load().gkrgpu_elapsed_ms(self.handle, a, b, ctypes.byref(ms)))
+        return ms.value
+
+    def transfer_stats(self):
+        h, d = ctypes.c_uint64(), ctypes.c_uint64()
+        _lib.check(_lib.load().gkrgpu_transfer_stats(self.handle, ctypes.byref(h), ctypes.byref(d)))
+        return h.value, d.value
+
+
+class HostBuffer:
+    """Pinned host memory (gkrgpu_host_alloc) viewed as a numpy array."""
+
+    def __init__(self, nbytes: int, dtype=np.uint8):
+        p = ctypes.c_void_p()
+        _lib.check(_lib.load().gkrgpu_host_alloc(nbytes, ctypes.byref(p)))
+        self.ptr = p.value
+        self.nbytes = nbytes
+        self.array = np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(self.ptr)).view(dtype)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            _lib.load().gkrgpu_host_free(ctypes.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class DeviceBuffer:
+    """Device memory owned through a context (gkrgpu_device_alloc)."""
+
+    def __init__(self, ctx: Context, nbytes: int):
+        p = ctypes.c_void_p()
+        _lib.check(_lib.load().gkrgpu_device_alloc(ctx.handle, nbytes, ctypes.byref(p)))
+        self.ctx, self.ptr, self.nbytes = ctx, p.value, nbytes
+
+    def upload(self, host_array):
+        a = np.ascontiguousarray(host_array)
+        _lib.check(_lib.load().gkrgpu_memcpy_h2d(self.ctx.handle, ctypes.c_void_p(self.ptr), a.ctypes.data, a.nbytes))
+
+    def free(self):
+        if self.ptr:
+            _lib.load().gkrgpu_device_free(self.ctx.handle, ctypes.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
 
 class Prover:
     """gkr::Prover (include/LinearGKR/LinearGKR.hpp:34-91) on the GPU."""

@@ -124,6 +124,14 @@ int gkrgpu_kernel_stats(gkrgpu_ctx* ctx, gkrgpu_kernel_stat* out, int cap);
  * CTA budget of the reducing kernels.  0 keeps the current value. */
 int gkrgpu_set_tile(gkrgpu_ctx* ctx, uint32_t threads_per_row, uint32_t block, uint32_t ctas);
 
+/* Timing markers: gkrgpu_mark records CUDA event `slot` (0..63) on the context's stream;
+ * gkrgpu_elapsed_ms waits for `to_slot` and returns the device time between the two. */
+int gkrgpu_mark(gkrgpu_ctx* ctx, int slot);
+int gkrgpu_elapsed_ms(gkrgpu_ctx* ctx, int from_slot, int to_slot, double* ms);
+
+/* Bytes the library copied host->device and device->host since the last reset. */
+int gkrgpu_transfer_stats(gkrgpu_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
+
 #ifdef __cplusplus
 }
 #endif
