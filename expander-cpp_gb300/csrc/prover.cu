@@ -860,6 +860,52 @@ int gkrgpu_prove_device(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
                        claimed_v);
 }
 
+int gkrgpu_eval_multilinear(gkrgpu_ctx* ctx, const uint32_t* d_evals, uint32_t nb_vars, uint32_t n_copies,
+                            const uint32_t* r, int n_points, uint32_t* out) {
+    return guarded([&] {
+        check_ctx(ctx);
+        if (!d_evals || !r || !out) fail(GKRGPU_ERR_INVALID, "null buffer");
+        if ((uintptr_t)d_evals & 15) fail(GKRGPU_ERR_INVALID, "d_evals must be 16-byte aligned");
+        if (n_points < 1 || n_points > 3) fail(GKRGPU_ERR_INVALID, "n_points must be in [1, 3]");
+        if (nb_vars > 30) fail(GKRGPU_ERR_INVALID, "nb_vars must be <= 30");
+        if (n_copies < 4 || n_copies % 4 || n_copies > (1u << 16))
+            fail(GKRGPU_ERR_INVALID, "n_copies must be a multiple of 4 in [4, 65536]");
+        for (int j = 0; j < n_points; j++)
+            for (uint32_t t = 0; t < nb_vars; t++)
+                if (r[(size_t)j * nb_vars + t] >= m31::P) fail(GKRGPU_ERR_INVALID, "point coordinate >= p");
+        const Geo g = ctx->geo(n_copies);
+        if (g.tpr * ((n_copies / 4) / g.tpr) != n_copies / 4) fail(GKRGPU_ERR_INVALID, "no row tile divides n_copies");
+        DeviceGuard dg(ctx->device);
+        const uint64_t rows = 1ull << nb_vars, rowb = (uint64_t)n_copies * 4;
+        ctx->eqc.ensure(n_points * rows * 4, "eq table");
+        if (ctx->acc.cap < 9ull * n_copies * 8) {
+            ctx->acc.ensure(9ull * n_copies * 8, "reduction scratch");
+            ck(cudaMemsetAsync(ctx->acc.p, 0, ctx->acc.cap, ctx->stream), "cudaMemsetAsync");
+        }
+        if (!ctx->ticket.p) {
+            ctx->ticket.ensure(256, "ticket");
+            ck(cudaMemsetAsync(ctx->ticket.p, 0, ctx->ticket.cap, ctx->stream), "cudaMemsetAsync");
+        }
+        ctx->cv.ensure(3 * rowb, "claims");
+        ctx->h_cv.ensure(3 * rowb, "pinned claims");
+        EqArgs a;
+        memset(&a, 0, sizeof(a));
+        for (int j = 0; j < n_points; j++) memcpy(a.r1[j], r + (size_t)j * nb_vars, 4 * nb_vars);
+        a.f1 = 1u;
+        a.nvars = nb_vars;
+        a.reps = n_points;
+        ctx->launch(K_EQ, 4.0 * n_points * rows, [&] { return launch_eq(ctx->eqc.as<uint32_t>(), a, ctx->stream); });
+        ctx->launch(K_WSUM, 4.0 * n_copies * rows + 4.0 * n_points * rows, [&] {
+            return launch_wsum(n_points, d_evals, rows, ctx->eqc.as<uint32_t>(), g, ctx->block, ctx->cta_budget(),
+                               ctx->red(), ctx->cv.as<uint32_t>(), ctx->stream);
+        });
+        ctx->copy(ctx->h_cv.p, ctx->cv.p, n_points * rowb, cudaMemcpyDeviceToHost, "result readback");
+        ctx->sync();
+        memcpy(out, ctx->h_cv.p, n_points * rowb);
+        if (ctx->timing) ctx->resolve_events();
+    });
+}
+
 int gkrgpu_device_alloc(gkrgpu_ctx* ctx, uint64_t bytes, void** out) {
     return guarded([&] {
         check_ctx(ctx);

@@ -156,6 +156,15 @@ class Context:
                                            out_buf.ctypes.data, out_buf.nbytes, ctypes.byref(plen), cv.ctypes.data))
         return cv, plen.value
 
+    def eval_multilinear(self, d_evals: int, nb_vars: int, n_copies: int, points):
+        """eval_multilinear of the device table at d_evals (2^nb_vars rows) at 1..3 points;
+        returns (n_points, n_copies) uint32."""
+        pts = np.ascontiguousarray(np.atleast_2d(points), dtype=np.uint32)
+        out = np.empty((pts.shape[0], n_copies), np.uint32)
+        _lib.check(_lib.load().gkrgpu_eval_multilinear(self.handle, ctypes.c_void_p(d_evals), nb_vars, n_copies,
+                                                       pts.ctypes.data, pts.shape[0], out.ctypes.data))
+        return out
+
     def set_timing(self, enabled: bool):
         _lib.check(_lib.load().gkrgpu_set_timing(self.handle, int(enabled)))
 

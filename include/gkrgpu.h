@@ -105,6 +105,16 @@ int gkrgpu_prove_device(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
                         const uint32_t* d_input, uint8_t* proof_out, uint64_t proof_cap, uint64_t* proof_len,
                         uint32_t* claimed_v);
 
+/* eval_multilinear (include/poly_commit/poly.hpp:88-104) of a device table d_evals of
+ * 2^nb_vars rows at n_points (1..3) points: r is a host array of n_points x nb_vars
+ * canonical values, out (host) receives n_points rows of n_copies lanes, row j being
+ * sum_z eq(r_j, z) * evals[z].  This is RawPC::verify's check value
+ * (include/poly_commit/raw.hpp:75-78) and gkr_prove's output claim
+ * (include/LinearGKR/gkr.hpp:52-55).  The eq tables and the reduction scratch live in
+ * the context's workspace. */
+int gkrgpu_eval_multilinear(gkrgpu_ctx* ctx, const uint32_t* d_evals, uint32_t nb_vars, uint32_t n_copies,
+                            const uint32_t* r, int n_points, uint32_t* out);
+
 /* Device / pinned host buffers for callers without a CUDA allocator of their own. */
 int gkrgpu_device_alloc(gkrgpu_ctx* ctx, uint64_t bytes, void** out);
 int gkrgpu_device_free(gkrgpu_ctx* ctx, void* p);
