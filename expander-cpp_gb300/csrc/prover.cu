@@ -747,6 +747,11 @@ int prove_entry(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copie
 
 }  // namespace
 
+namespace gkrgpu {
+// Records the calling thread's error text (shared with the other translation units).
+void set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+}  // namespace gkrgpu
+
 // ------------------------------------------------------------------ C ABI
 extern "C" {
 

@@ -115,6 +115,23 @@ int gkrgpu_prove_device(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
 int gkrgpu_eval_multilinear(gkrgpu_ctx* ctx, const uint32_t* d_evals, uint32_t nb_vars, uint32_t n_copies,
                             const uint32_t* r, int n_points, uint32_t* out);
 
+/* gkrgpu_eval_multilinear without any allocation, for callers that cannot allocate device
+ * memory: e.g. a verifier living in a process whose device memory is already reserved by
+ * another framework's caching allocator, or code where cudaMalloc/cudaFree (which can
+ * synchronize the whole device) are not allowed.  No counterpart in the reference.
+ * Same result as gkrgpu_eval_multilinear, but the output d_out is a caller-owned device
+ * buffer of n_points x n_copies u32 and no context is needed: the work runs on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream) of the current device and the call
+ * returns when it has finished.  Its scratch is a fixed 3.1 MiB region inside the library
+ * (held by every GPU that loads the library until the process exits), so the limits are
+ * nb_vars <= 18, n_copies <= 4096 (a multiple of 4) and n_points <= 3; larger sizes are
+ * rejected with GKRGPU_ERR_INVALID.  The first call on a device looks up the scratch
+ * address; make that first call before any stream capture.  All calls share the one
+ * scratch region: calls that overlap on the GPU (from several host threads or streams)
+ * race and must be serialized by the caller. */
+int gkrgpu_eval_multilinear_noalloc(const uint32_t* d_evals, uint32_t nb_vars, uint32_t n_copies,
+                                    const uint32_t* r, int n_points, uint32_t* d_out, void* stream);
+
 /* Device / pinned host buffers for callers without a CUDA allocator of their own. */
 int gkrgpu_device_alloc(gkrgpu_ctx* ctx, uint64_t bytes, void** out);
 int gkrgpu_device_free(gkrgpu_ctx* ctx, void* p);
