@@ -17,12 +17,17 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <deque>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gkrgpu.h"
@@ -162,6 +167,27 @@ struct gkrgpu_circuit {
     }
 };
 
+// ------------------------------------------------------------------ jobs
+// One queued Prover::prove (gkrgpu_prove_submit).  The host stage fills `ts`; the device
+// stage resumes from it.  The submitting thread waits on `cv` for done && host_done.
+struct gkrgpu_job {
+    const gkrgpu_circuit* circuit = nullptr;
+    uint32_t N = 0;
+    int grinding = 10, R = 3, marker = -1;
+    const uint32_t* h_input = nullptr;
+    const uint32_t* d_input = nullptr;
+    uint8_t* proof_out = nullptr;
+    uint64_t proof_len = 0;
+    uint32_t* claimed_v = nullptr;
+
+    TranscriptState ts;
+    bool host_done = false, done = false;
+    int host_rc = GKRGPU_OK, rc = GKRGPU_OK;
+    std::string host_err, err;
+    std::mutex m;
+    std::condition_variable cv;
+};
+
 // ------------------------------------------------------------------ context
 struct gkrgpu_ctx {
     int device = 0;
@@ -169,17 +195,45 @@ struct gkrgpu_ctx {
     cudaStream_t stream = nullptr;
     uint32_t tpr_max = 32, block = 256, ctas = 0;
 
+    // job pipeline: one device-stage worker, host-stage workers
+    std::mutex qm;
+    std::condition_variable qcv;
+    std::deque<gkrgpu_job*> host_q, gpu_q;
+    std::vector<std::thread> workers;
+    bool stopping = false, gpu_busy = false;
+    int host_workers = 2;
+    void start_workers();
+    void shutdown() {
+        {
+            std::lock_guard<std::mutex> lk(qm);
+            stopping = true;
+        }
+        qcv.notify_all();
+        for (auto& t : workers) t.join();
+        workers.clear();
+    }
+    // Waits until no device stage is queued or running.
+    void drain() {
+        std::unique_lock<std::mutex> lk(qm);
+        qcv.wait(lk, [&] { return gpu_q.empty() && !gpu_busy; });
+    }
+
     DevBuf vals, eqc, eqrx, a4, w4, acc, ticket, evals, vx, cv, flag;
     DevBuf fA[3], fB[3], hg0[3], hgA[3], sb[2];
     DevBuf h_evals, h_rows, h_vx, h_cv, h_flag;  // pinned
 
     // launch accounting
     bool timing = false;
-    uint64_t h2d_bytes = 0, d2h_bytes = 0;
+    std::atomic<uint64_t> h2d_bytes{0}, d2h_bytes{0};
     cudaEvent_t markers[64] = {};
+    // Totals (read by gkrgpu_kernel_stats under stats_m); each job's launches accumulate
+    // in job_* and are folded in when the job ends, so snapshots fall on job boundaries.
+    std::mutex stats_m;
     uint64_t launches[K_NUM_KERNELS] = {};
     double ms[K_NUM_KERNELS] = {};
     double bytes[K_NUM_KERNELS] = {};
+    uint64_t job_launches[K_NUM_KERNELS] = {};
+    double job_bytes[K_NUM_KERNELS] = {};
     struct Rec {
         int kid;
         size_t e0, e1;
@@ -223,23 +277,41 @@ struct gkrgpu_ctx {
             ck(cudaEventRecord(events[e0], stream), "cudaEventRecord");
         }
         ck(f(), kKernelNames[kid]);
-        launches[kid]++;
-        bytes[kid] += algo_bytes;
+        job_launches[kid]++;
+        job_bytes[kid] += algo_bytes;
         if (timing) {
             const size_t e1 = next_event();
             ck(cudaEventRecord(events[e1], stream), "cudaEventRecord");
             recs.push_back({kid, e0, e1});
         }
     }
-    // Folds recorded event pairs into per-kernel times; the stream must be idle.
+    // Folds the finished job's launch counts, bytes and event times into the totals; the
+    // stream must be idle.
     void resolve_events() {
+        double t_ms[K_NUM_KERNELS] = {};
         for (const Rec& r : recs) {
             float t = 0.f;
             ck(cudaEventElapsedTime(&t, events[r.e0], events[r.e1]), "cudaEventElapsedTime");
-            ms[r.kid] += t;
+            t_ms[r.kid] += t;
         }
         recs.clear();
         ev_used = 0;
+        std::lock_guard<std::mutex> lk(stats_m);
+        for (int k = 0; k < K_NUM_KERNELS; k++) {
+            launches[k] += job_launches[k];
+            bytes[k] += job_bytes[k];
+            ms[k] += t_ms[k];
+            job_launches[k] = 0;
+            job_bytes[k] = 0;
+        }
+    }
+    void discard_job_stats() {
+        recs.clear();
+        ev_used = 0;
+        for (int k = 0; k < K_NUM_KERNELS; k++) {
+            job_launches[k] = 0;
+            job_bytes[k] = 0;
+        }
     }
     void sync() { ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
     // Stream-ordered copy, counted in the transfer statistics.
@@ -625,30 +697,23 @@ struct Prover {
         for (int j = 0; j < R; j++) t.append(vy.data() + (size_t)j * N, rowb);
     }
 
-    void prove(const uint32_t* h_input, const uint32_t* d_input, int grinding_bits, uint8_t* proof_out,
-               uint32_t* claimed_v) {
-        const size_t L = C.layers.size();
-        const uint64_t rowb = (uint64_t)N * 4;
-        const uint64_t in_bytes = C.in_rows(0) * rowb;
+    // Device front half of a proof: input upload and check, Circuit::evaluate of every layer.
+    // Asynchronous on the context's stream; it needs no transcript.
+    void device_front(const uint32_t* h_input, const uint32_t* d_input) {
+        const uint64_t in_bytes = C.in_rows(0) * (uint64_t)N * 4;
         reserve(d_input == nullptr);
         layout_values(d_input);
-        if (h_input)
-            c.copy(vals[0], h_input, in_bytes, cudaMemcpyHostToDevice, "input upload");
+        if (h_input) c.copy(vals[0], h_input, in_bytes, cudaMemcpyHostToDevice, "input upload");
         check_input();
         evaluate();
+    }
 
-        // RAW commitment: the input layer verbatim (raw.hpp:19-27,61-71), hashed by the
-        // first challenge of grind while the device evaluates the circuit.
-        Transcript t(proof_out, ~0ull);
-        if (h_input) {
-            t.append(h_input, in_bytes);
-        } else {
-            c.copy(t.tail(), d_input, in_bytes, cudaMemcpyDeviceToHost, "commitment readback");
-            c.sync();
-            require_canonical();
-            t.appended(in_bytes);
-        }
-        grind(t, grinding_bits);
+    // Device back half: gkr_prove from the transcript state left by the host stage (RAW
+    // commitment + grinding), writing the rest of the proof and the claimed values.
+    void device_back(const TranscriptState& ts, uint8_t* proof_out, uint32_t* claimed_v) {
+        const size_t L = C.layers.size();
+        const uint64_t rowb = (uint64_t)N * 4;
+        Transcript t(proof_out, ts);
 
         // gkr_prove (gkr.hpp:42-55): rz1 challenges (i outer, j inner), rz2 = 0, alpha = 1, beta = 0.
         uint32_t rz1[3][32], rz2[3][32], rx[3][32], ry[3][32];
@@ -683,7 +748,7 @@ struct Prover {
         }
         // RawPC::open: the openings are empty (raw.hpp:61-66, LinearGKR.hpp:77-86).
         c.sync();
-        if (c.timing) c.resolve_events();
+        c.resolve_events();
     }
 
     void evaluate_only(const uint32_t* h_input, uint32_t* out, bool all_layers) {
@@ -701,7 +766,7 @@ struct Prover {
         } else {
             ck(cudaMemcpy(out, vals[L], C.out_rows(L - 1) * rowb, cudaMemcpyDeviceToHost), "output readback");
         }
-        if (c.timing) c.resolve_events();
+        c.resolve_events();
     }
 };
 
@@ -726,26 +791,206 @@ uint64_t proof_bytes(const gkrgpu_circuit* c, uint32_t N, int R) {
     return c->in_rows(0) * N * 4 + 32 + rows * N * 4;
 }
 
+// ------------------------------------------------------------------ job pipeline
+// A proof is two stages: the host stage (RAW commitment bytes into the proof buffer, their
+// SHA-256, grinding) and the device stage (upload, evaluate, then gkr_prove resuming the
+// transcript).  The device stage of proof k runs on the GPU worker while host workers
+// hash the commitments of proofs k+1, k+2, ...; device stages run one at a time in
+// submission order because they share the context's workspace.
+
+// Copies n bytes in helper threads while this thread hashes the source.
+void parallel_copy_and_hash(uint8_t* dst, const uint8_t* src, uint64_t n, uint8_t digest[32]) {
+    const unsigned k = n >= (64ull << 20) ? 4 : (n >= (4ull << 20) ? 2 : 0);
+    std::vector<std::thread> th;
+    if (k) {
+        const uint64_t chunk = (n + k - 1) / k;
+        for (unsigned i = 0; i < k; i++) {
+            const uint64_t a = i * chunk, b = std::min<uint64_t>(n, a + chunk);
+            if (a < b) th.emplace_back([=] { memcpy(dst + a, src + a, b - a); });
+        }
+    } else {
+        memcpy(dst, src, n);
+    }
+    sha256(src, n, digest);
+    for (auto& t : th) t.join();
+}
+
+TranscriptState host_stage(gkrgpu_ctx& c, gkrgpu_job& j, cudaStream_t s) {
+    const uint64_t in_bytes = j.circuit->in_rows(0) * (uint64_t)j.N * 4;
+    uint8_t d[32];
+    if (j.h_input) {
+        parallel_copy_and_hash(j.proof_out, reinterpret_cast<const uint8_t*>(j.h_input), in_bytes, d);
+    } else {
+        ck(cudaMemcpyAsync(j.proof_out, j.d_input, in_bytes, cudaMemcpyDeviceToHost, s), "commitment readback");
+        ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        c.d2h_bytes += in_bytes;
+        sha256(j.proof_out, in_bytes, d);
+    }
+    Transcript t(j.proof_out, ~0ull);
+    t.appended_prehashed(in_bytes, d);
+    grind(t, j.grinding);
+    return t.state();
+}
+
+void host_worker(gkrgpu_ctx* c) {
+    cudaSetDevice(c->device);
+    cudaStream_t s = nullptr;
+    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    for (;;) {
+        gkrgpu_job* j;
+        {
+            std::unique_lock<std::mutex> lk(c->qm);
+            c->qcv.wait(lk, [&] { return c->stopping || !c->host_q.empty(); });
+            if (c->host_q.empty()) break;
+            j = c->host_q.front();
+            c->host_q.pop_front();
+        }
+        int rc = GKRGPU_OK;
+        std::string err;
+        try {
+            if (!s) fail(GKRGPU_ERR_CUDA, "host worker stream creation failed");
+            j->ts = host_stage(*c, *j, s);
+        } catch (const Error& e) {
+            rc = e.code;
+            err = e.what();
+        } catch (const std::exception& e) {
+            rc = GKRGPU_ERR_STATE;
+            err = e.what();
+        }
+        {
+            std::lock_guard<std::mutex> lk(j->m);
+            j->host_rc = rc;
+            j->host_err = err;
+            j->host_done = true;
+        }
+        j->cv.notify_all();
+    }
+    if (s) cudaStreamDestroy(s);
+}
+
+void gpu_worker(gkrgpu_ctx* c) {
+    cudaSetDevice(c->device);
+    for (;;) {
+        gkrgpu_job* j;
+        {
+            std::unique_lock<std::mutex> lk(c->qm);
+            c->qcv.wait(lk, [&] { return c->stopping || !c->gpu_q.empty(); });
+            if (c->gpu_q.empty()) break;
+            j = c->gpu_q.front();
+            c->gpu_q.pop_front();
+            c->gpu_busy = true;
+        }
+        int rc = GKRGPU_OK;
+        std::string err;
+        try {
+            Prover p(*c, *j->circuit, j->N, j->R);
+            p.device_front(j->h_input, j->d_input);
+            {
+                std::unique_lock<std::mutex> lk(j->m);
+                j->cv.wait(lk, [&] { return j->host_done; });
+            }
+            if (j->host_rc) throw Error(j->host_rc, j->host_err);
+            p.device_back(j->ts, j->proof_out, j->claimed_v);
+            if (j->marker >= 0) {
+                if (!c->markers[j->marker]) ck(cudaEventCreate(&c->markers[j->marker]), "cudaEventCreate");
+                ck(cudaEventRecord(c->markers[j->marker], c->stream), "cudaEventRecord");
+            }
+        } catch (const Error& e) {
+            rc = e.code;
+            err = e.what();
+        } catch (const std::exception& e) {
+            rc = GKRGPU_ERR_STATE;
+            err = e.what();
+        }
+        if (rc != GKRGPU_OK) {
+            cudaStreamSynchronize(c->stream);
+            c->discard_job_stats();
+        }
+        {
+            std::lock_guard<std::mutex> lk(j->m);
+            j->rc = rc;
+            j->err = err;
+            j->done = true;
+        }
+        j->cv.notify_all();
+        {
+            std::lock_guard<std::mutex> lk(c->qm);
+            c->gpu_busy = false;
+        }
+        c->qcv.notify_all();
+    }
+}
+
+gkrgpu_job* submit(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
+                   const uint32_t* h_input, const uint32_t* d_input, uint8_t* proof_out, uint64_t proof_cap,
+                   uint32_t* claimed_v, int marker, uint64_t* need_out) {
+    check_run(ctx, circuit, n_copies);
+    if (grinding_bits < 0 || grinding_bits > 30) fail(GKRGPU_ERR_INVALID, "grinding_bits must be in [0, 30]");
+    const int R = reps_for(grinding_bits);
+    if (R < 1 || R > 3) fail(GKRGPU_ERR_INVALID, "grinding_bits %d gives %d repetitions (1..3 supported)", grinding_bits, R);
+    if (!(h_input || d_input) || !proof_out || !claimed_v) fail(GKRGPU_ERR_INVALID, "null buffer");
+    if (d_input && ((uintptr_t)d_input & 15)) fail(GKRGPU_ERR_INVALID, "device input must be 16-byte aligned");
+    if (marker < -1 || marker >= 64) fail(GKRGPU_ERR_INVALID, "marker slot must be -1 or in [0, 64)");
+    const uint64_t need = proof_bytes(circuit, n_copies, R);
+    if (need_out) *need_out = need;
+    if (proof_cap < need)
+        fail(GKRGPU_ERR_CAPACITY, "proof needs %llu bytes, buffer has %llu", (unsigned long long)need,
+             (unsigned long long)proof_cap);
+    gkrgpu_job* j = new gkrgpu_job();
+    j->circuit = circuit;
+    j->N = n_copies;
+    j->grinding = grinding_bits;
+    j->R = R;
+    j->h_input = h_input;
+    j->d_input = d_input;
+    j->proof_out = proof_out;
+    j->proof_len = need;
+    j->claimed_v = claimed_v;
+    j->marker = marker;
+    ctx->start_workers();
+    {
+        std::lock_guard<std::mutex> lk(ctx->qm);
+        ctx->host_q.push_back(j);
+        ctx->gpu_q.push_back(j);
+    }
+    ctx->qcv.notify_all();
+    return j;
+}
+
+int wait_job(gkrgpu_job* j, uint64_t* proof_len) {
+    {
+        std::unique_lock<std::mutex> lk(j->m);
+        j->cv.wait(lk, [&] { return j->done && j->host_done; });
+    }
+    const int rc = j->rc;
+    if (rc != GKRGPU_OK) g_last_error = j->err;
+    if (proof_len) *proof_len = j->proof_len;
+    delete j;
+    return rc;
+}
+
 int prove_entry(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
                 const uint32_t* h_input, const uint32_t* d_input, uint8_t* proof_out, uint64_t proof_cap,
                 uint64_t* proof_len, uint32_t* claimed_v) {
-    return guarded([&] {
-        check_run(ctx, circuit, n_copies);
-        if (grinding_bits < 0 || grinding_bits > 30) fail(GKRGPU_ERR_INVALID, "grinding_bits must be in [0, 30]");
-        const int R = reps_for(grinding_bits);
-        if (R < 1 || R > 3) fail(GKRGPU_ERR_INVALID, "grinding_bits %d gives %d repetitions (1..3 supported)", grinding_bits, R);
-        if (!(h_input || d_input) || !proof_out || !proof_len || !claimed_v) fail(GKRGPU_ERR_INVALID, "null buffer");
-        const uint64_t need = proof_bytes(circuit, n_copies, R);
-        *proof_len = need;
-        if (proof_cap < need) fail(GKRGPU_ERR_CAPACITY, "proof needs %llu bytes, buffer has %llu",
-                                   (unsigned long long)need, (unsigned long long)proof_cap);
-        DeviceGuard dg(ctx->device);
-        Prover p(*ctx, *circuit, n_copies, R);
-        p.prove(h_input, d_input, grinding_bits, proof_out, claimed_v);
+    gkrgpu_job* j = nullptr;
+    const int rc = guarded([&] {
+        if (!proof_len) fail(GKRGPU_ERR_INVALID, "null proof_len");
+        j = submit(ctx, circuit, n_copies, grinding_bits, h_input, d_input, proof_out, proof_cap, claimed_v, -1,
+                   proof_len);
     });
+    if (rc != GKRGPU_OK) return rc;
+    return wait_job(j, proof_len);
 }
 
 }  // namespace
+
+void gkrgpu_ctx::start_workers() {
+    std::lock_guard<std::mutex> lk(qm);
+    if (!workers.empty()) return;
+    stopping = false;
+    workers.emplace_back(gpu_worker, this);
+    for (int i = 0; i < host_workers; i++) workers.emplace_back(host_worker, this);
+}
 
 namespace gkrgpu {
 // Records the calling thread's error text (shared with the other translation units).
@@ -788,6 +1033,7 @@ int gkrgpu_create(int device, gkrgpu_ctx** out) {
 void gkrgpu_destroy(gkrgpu_ctx* ctx) {
     if (!ctx) return;
     try {
+        ctx->shutdown();
         delete ctx;
     } catch (...) {
     }
@@ -841,10 +1087,30 @@ int gkrgpu_evaluate(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_c
     return guarded([&] {
         check_run(ctx, circuit, n_copies);
         if (!input || !out) fail(GKRGPU_ERR_INVALID, "null buffer");
+        ctx->drain();
         DeviceGuard dg(ctx->device);
         Prover p(*ctx, *circuit, n_copies, 1);
         p.evaluate_only(input, out, all_layers != 0);
     });
+}
+
+int gkrgpu_prove_submit(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
+                        const uint32_t* input, int input_on_device, uint8_t* proof_out, uint64_t proof_cap,
+                        uint32_t* claimed_v, int marker_slot, gkrgpu_job** job) {
+    return guarded([&] {
+        if (!job) fail(GKRGPU_ERR_INVALID, "null job output");
+        *job = nullptr;
+        *job = submit(ctx, circuit, n_copies, grinding_bits, input_on_device ? nullptr : input,
+                      input_on_device ? input : nullptr, proof_out, proof_cap, claimed_v, marker_slot, nullptr);
+    });
+}
+
+int gkrgpu_prove_wait(gkrgpu_job* job, uint64_t* proof_len) {
+    if (!job) {
+        g_last_error = "null job";
+        return GKRGPU_ERR_INVALID;
+    }
+    return wait_job(job, proof_len);
 }
 
 int gkrgpu_prove(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
@@ -869,6 +1135,7 @@ int gkrgpu_eval_multilinear(gkrgpu_ctx* ctx, const uint32_t* d_evals, uint32_t n
                             const uint32_t* r, int n_points, uint32_t* out) {
     return guarded([&] {
         check_ctx(ctx);
+        ctx->drain();
         if (!d_evals || !r || !out) fail(GKRGPU_ERR_INVALID, "null buffer");
         if ((uintptr_t)d_evals & 15) fail(GKRGPU_ERR_INVALID, "d_evals must be 16-byte aligned");
         if (n_points < 1 || n_points > 3) fail(GKRGPU_ERR_INVALID, "n_points must be in [1, 3]");
@@ -907,7 +1174,7 @@ int gkrgpu_eval_multilinear(gkrgpu_ctx* ctx, const uint32_t* d_evals, uint32_t n
         ctx->copy(ctx->h_cv.p, ctx->cv.p, n_points * rowb, cudaMemcpyDeviceToHost, "result readback");
         ctx->sync();
         memcpy(out, ctx->h_cv.p, n_points * rowb);
-        if (ctx->timing) ctx->resolve_events();
+        ctx->resolve_events();
     });
 }
 
@@ -942,6 +1209,7 @@ int gkrgpu_host_free(void* p) {
 int gkrgpu_memcpy_h2d(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t bytes) {
     return guarded([&] {
         check_ctx(ctx);
+        ctx->drain();
         DeviceGuard dg(ctx->device);
         ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
         ctx->sync();
@@ -951,6 +1219,7 @@ int gkrgpu_memcpy_h2d(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t byte
 int gkrgpu_memcpy_d2h(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t bytes) {
     return guarded([&] {
         check_ctx(ctx);
+        ctx->drain();
         DeviceGuard dg(ctx->device);
         ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
         ctx->sync();
@@ -960,6 +1229,7 @@ int gkrgpu_memcpy_d2h(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t byte
 int gkrgpu_set_timing(gkrgpu_ctx* ctx, int enabled) {
     return guarded([&] {
         check_ctx(ctx);
+        ctx->drain();
         ctx->timing = enabled != 0;
     });
 }
@@ -967,13 +1237,14 @@ int gkrgpu_set_timing(gkrgpu_ctx* ctx, int enabled) {
 int gkrgpu_reset_stats(gkrgpu_ctx* ctx) {
     return guarded([&] {
         check_ctx(ctx);
+        ctx->drain();
+        ctx->discard_job_stats();
+        std::lock_guard<std::mutex> lk(ctx->stats_m);
         for (int k = 0; k < K_NUM_KERNELS; k++) {
             ctx->launches[k] = 0;
             ctx->ms[k] = 0;
             ctx->bytes[k] = 0;
         }
-        ctx->recs.clear();
-        ctx->ev_used = 0;
         ctx->h2d_bytes = ctx->d2h_bytes = 0;
     });
 }
@@ -1012,6 +1283,7 @@ int gkrgpu_transfer_stats(gkrgpu_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_by
 
 int gkrgpu_kernel_stats(gkrgpu_ctx* ctx, gkrgpu_kernel_stat* out, int cap) {
     if (!ctx) return -GKRGPU_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->stats_m);
     for (int k = 0; k < K_NUM_KERNELS && k < cap; k++) {
         out[k].name = kKernelNames[k];
         out[k].launches = ctx->launches[k];
@@ -1024,6 +1296,7 @@ int gkrgpu_kernel_stats(gkrgpu_ctx* ctx, gkrgpu_kernel_stat* out, int cap) {
 int gkrgpu_set_tile(gkrgpu_ctx* ctx, uint32_t threads_per_row, uint32_t block, uint32_t ctas) {
     return guarded([&] {
         check_ctx(ctx);
+        ctx->drain();
         const uint32_t b = block ? block : ctx->block;
         const uint32_t t = threads_per_row ? threads_per_row : ctx->tpr_max;
         if (b < 32 || b > 256 || b % 32) fail(GKRGPU_ERR_INVALID, "block must be a multiple of 32 in [32, 256]");

@@ -14,41 +14,64 @@
 
 namespace gkrgpu {
 
+// Position of a transcript: bytes written, start of the not-yet-hashed bytes, digest.
+struct TranscriptState {
+    uint64_t len = 0, hash_start = 0;
+    uint8_t digest[32] = {};
+};
+
 class Transcript {
    public:
-    Transcript(uint8_t* buf, uint64_t cap) : buf_(buf), cap_(cap) { memset(digest_, 0, 32); }
+    Transcript(uint8_t* buf, uint64_t cap) : buf_(buf), cap_(cap) {}
+    // Resumes a transcript over the same buffer (e.g. on another thread).
+    Transcript(uint8_t* buf, const TranscriptState& s) : buf_(buf), cap_(~0ull), s_(s) {}
 
-    uint64_t size() const { return len_; }
-    uint8_t* tail() { return buf_ + len_; }
+    const TranscriptState& state() const { return s_; }
+    uint64_t size() const { return s_.len; }
+    uint8_t* tail() { return buf_ + s_.len; }
 
     // Appends n bytes (the caller has checked the capacity: the proof size is exact).
     void append(const void* p, uint64_t n) {
-        memcpy(buf_ + len_, p, n);
-        len_ += n;
+        memcpy(buf_ + s_.len, p, n);
+        s_.len += n;
     }
     // Marks n bytes already written at tail() as appended.
-    void appended(uint64_t n) { len_ += n; }
+    void appended(uint64_t n) { s_.len += n; }
+    // Marks n bytes already written at tail() as appended when their SHA-256 `d` was computed
+    // elsewhere (from the same bytes); the next challenge uses it if nothing else was appended.
+    void appended_prehashed(uint64_t n, const uint8_t d[32]) {
+        s_.len += n;
+        memcpy(pre_, d, 32);
+        pre_from_ = s_.len - n;
+        pre_to_ = s_.len;
+        has_pre_ = true;
+    }
 
     uint32_t challenge() {
-        if (len_ > hash_start_) {
-            sha256(buf_ + hash_start_, len_ - hash_start_, digest_);
-            hash_start_ = len_;
+        if (has_pre_ && s_.hash_start == pre_from_ && s_.len == pre_to_) {
+            memcpy(s_.digest, pre_, 32);
+            s_.hash_start = s_.len;
+            has_pre_ = false;
+        } else if (s_.len > s_.hash_start) {
+            sha256(buf_ + s_.hash_start, s_.len - s_.hash_start, s_.digest);
+            s_.hash_start = s_.len;
         } else {
             uint8_t d[32];
-            sha256(digest_, 32, d);
-            memcpy(digest_, d, 32);
+            sha256(s_.digest, 32, d);
+            memcpy(s_.digest, d, 32);
         }
         uint32_t x;
-        memcpy(&x, digest_, 4);
+        memcpy(&x, s_.digest, 4);
         return m31::from_u32(x);
     }
 
    private:
     uint8_t* buf_;
     uint64_t cap_;
-    uint64_t len_ = 0;
-    uint64_t hash_start_ = 0;
-    uint8_t digest_[32];
+    TranscriptState s_;
+    uint8_t pre_[32];
+    uint64_t pre_from_ = 0, pre_to_ = 0;
+    bool has_pre_ = false;
 };
 
 // grind (include/LinearGKR/LinearGKR.hpp:13-32): 256/31 = 8 challenges written at 4-byte

@@ -52,6 +52,8 @@ SIGNATURES = [
     ("gkrgpu_evaluate", _I, [_P, _P, _U32, _P, _P, _I]),
     ("gkrgpu_prove", _I, [_P, _P, _U32, _I, _P, _P, _U64, ctypes.POINTER(_U64), _P]),
     ("gkrgpu_prove_device", _I, [_P, _P, _U32, _I, _P, _P, _U64, ctypes.POINTER(_U64), _P]),
+    ("gkrgpu_prove_submit", _I, [_P, _P, _U32, _I, _P, _I, _P, _U64, _P, _I, ctypes.POINTER(_P)]),
+    ("gkrgpu_prove_wait", _I, [_P, ctypes.POINTER(_U64)]),
     ("gkrgpu_eval_multilinear", _I, [_P, _P, _U32, _U32, _P, _I, _P]),
     ("gkrgpu_eval_multilinear_noalloc", _I, [_P, _U32, _U32, _P, _I, _P, _P]),
     ("gkrgpu_device_alloc", _I, [_P, _U64, ctypes.POINTER(_P)]),

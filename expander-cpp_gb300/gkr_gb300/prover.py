@@ -156,6 +156,29 @@ class Context:
                                            out_buf.ctypes.data, out_buf.nbytes, ctypes.byref(plen), cv.ctypes.data))
         return cv, plen.value
 
+    def submit(self, dc: DeviceCircuit, witness, proof_buf, claimed_buf, grinding_bits=10, d_input=None,
+               marker=-1):
+        """gkrgpu_prove_submit: queues one proof and returns a Job.  The witness (host array)
+        or d_input (device address), proof_buf and claimed_buf must outlive the job."""
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        if d_input is not None:
+            src, on_dev, n, keep = ctypes.c_void_p(d_input), 1, claimed_buf.shape[1], None
+        else:
+            keep = np.ascontiguousarray(witness, dtype=np.uint32)
+            src, on_dev, n = keep.ctypes.data, 0, keep.shape[1]
+        _lib.check(lib.gkrgpu_prove_submit(self.handle, dc.handle, n, grinding_bits, src, on_dev,
+                                           proof_buf.ctypes.data, proof_buf.nbytes, claimed_buf.ctypes.data, marker,
+                                           ctypes.byref(h)))
+        return Job(h, (keep, proof_buf, claimed_buf))
+
+    def wait(self, job: "Job") -> int:
+        """gkrgpu_prove_wait: blocks until the job is done; returns the proof length."""
+        plen = ctypes.c_uint64()
+        h, job.handle = job.handle, None
+        _lib.check(_lib.load().gkrgpu_prove_wait(h, ctypes.byref(plen)))
+        return plen.value
+
     def eval_multilinear(self, d_evals: int, nb_vars: int, n_copies: int, points):
         """eval_multilinear of the device table at d_evals (2^nb_vars rows) at 1..3 points;
         returns (n_points, n_copies) uint32."""
@@ -194,6 +217,14 @@ class Context:
         h, d = ctypes.c_uint64(), ctypes.c_uint64()
         _lib.check(_lib.load().gkrgpu_transfer_stats(self.handle, ctypes.byref(h), ctypes.byref(d)))
         return h.value, d.value
+
+
+class Job:
+    """A queued proof (gkrgpu_job); keeps its buffers alive until waited on."""
+
+    def __init__(self, handle, buffers):
+        self.handle = handle
+        self.buffers = buffers
 
 
 class HostBuffer:

@@ -105,6 +105,22 @@ int gkrgpu_prove_device(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
                         const uint32_t* d_input, uint8_t* proof_out, uint64_t proof_cap, uint64_t* proof_len,
                         uint32_t* claimed_v);
 
+/* Pipelined Prover::prove.  gkrgpu_prove_submit queues one proof and returns at once; its
+ * host stage (RAW commitment bytes, their SHA-256, grinding) runs on a host worker while
+ * earlier proofs' device stages run on the GPU, and device stages run one at a time in
+ * submission order.  The input (host memory, or device memory with input_on_device = 1),
+ * proof_out and claimed_v must stay valid until gkrgpu_prove_wait returns.  With
+ * marker_slot >= 0 the device stage's end is recorded as timing marker `marker_slot`
+ * (gkrgpu_elapsed_ms).  gkrgpu_prove_wait blocks until the job is finished, frees it and
+ * returns its status; proof_len receives the proof length.  gkrgpu_prove and
+ * gkrgpu_prove_device are submit + wait.  No counterpart in the reference (one proof per
+ * thread there, bench_keccak.cpp:82-93). */
+typedef struct gkrgpu_job gkrgpu_job;
+int gkrgpu_prove_submit(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
+                        const uint32_t* input, int input_on_device, uint8_t* proof_out, uint64_t proof_cap,
+                        uint32_t* claimed_v, int marker_slot, gkrgpu_job** job);
+int gkrgpu_prove_wait(gkrgpu_job* job, uint64_t* proof_len);
+
 /* eval_multilinear (include/poly_commit/poly.hpp:88-104) of a device table d_evals of
  * 2^nb_vars rows at n_points (1..3) points: r is a host array of n_points x nb_vars
  * canonical values, out (host) receives n_points rows of n_copies lanes, row j being
@@ -141,8 +157,11 @@ int gkrgpu_memcpy_h2d(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t byte
 int gkrgpu_memcpy_d2h(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t bytes);
 
 /* Launch accounting.  With timing on, every kernel launch is bracketed by CUDA events on
- * the context's stream.  gkrgpu_kernel_stats fills up to cap entries (one per kernel
- * kind) and returns how many kinds exist; gkrgpu_reset_stats clears the counters. */
+ * the context's stream.  Counts and times are added to the totals when each proof (or
+ * other call) finishes, so gkrgpu_kernel_stats, which may be called while proofs are in
+ * flight, always reads whole proofs; it fills up to cap entries (one per kernel kind) and
+ * returns how many kinds exist.  gkrgpu_set_timing and gkrgpu_reset_stats first wait for
+ * queued proofs to finish. */
 int gkrgpu_set_timing(gkrgpu_ctx* ctx, int enabled);
 int gkrgpu_reset_stats(gkrgpu_ctx* ctx);
 int gkrgpu_kernel_stats(gkrgpu_ctx* ctx, gkrgpu_kernel_stat* out, int cap);

@@ -111,3 +111,51 @@ def test_prover_api_mirror(ctx, oracle):
     assert isinstance(proof, Proof)
     assert sha(proof.bytes) == GOLDEN["gkr_test_shape_n16"]["proof_sha256"]
     assert oracle.verify(circ, w, cv, proof.bytes)
+
+
+def test_pipelined_jobs_are_byte_identical(ctx):
+    """Several proofs in flight (host stages overlapping device stages, mixed shapes and copy
+    counts); each must still reproduce its reference golden, in any completion order."""
+    names = ["cfg1_n16", "lanes1024", "mixed_widths_n16", "width_one_n8", "lanes48", "cfg1_n8"]
+    built = [cases.build(n) for n in names]
+    dcs = [ctx.load(c) for c, _, _ in built]
+    jobs = []
+    for (c, w, g), dc in zip(built, dcs):
+        pb = np.empty(dc.proof_size(w.shape[1], g), np.uint8)
+        cb = np.empty((3, w.shape[1]), np.uint32)
+        jobs.append((ctx.submit(dc, w, pb, cb, grinding_bits=g), pb, cb))
+    for name, (job, pb, cb) in zip(names, jobs):
+        n = ctx.wait(job)
+        assert sha(pb[:n].tobytes()) == GOLDEN[name]["proof_sha256"], name
+        assert sha(cb.tobytes()) == GOLDEN[name]["claimed_v_sha256"], name
+
+
+def test_failing_job_does_not_disturb_the_pipeline(ctx):
+    from gkr_gb300._lib import GkrGpuError
+    good = cases.build("cfg1_n16")
+    bad_w = good[1].copy()
+    bad_w[0, 0] = gc.P
+    dc = ctx.load(good[0])
+    bufs = [(np.empty(dc.proof_size(16), np.uint8), np.empty((3, 16), np.uint32)) for _ in range(3)]
+    j0 = ctx.submit(dc, good[1], *bufs[0])
+    j1 = ctx.submit(dc, bad_w, *bufs[1])
+    j2 = ctx.submit(dc, good[1], *bufs[2])
+    n0 = ctx.wait(j0)
+    with pytest.raises(GkrGpuError):
+        ctx.wait(j1)
+    n2 = ctx.wait(j2)
+    assert sha(bufs[0][0][:n0].tobytes()) == sha(bufs[2][0][:n2].tobytes()) == GOLDEN["cfg1_n16"]["proof_sha256"]
+
+
+def test_device_input_pipeline(ctx):
+    from gkr_gb300.prover import DeviceBuffer
+    circ, w, g = cases.build("lanes256")
+    dc = ctx.load(circ)
+    d = DeviceBuffer(ctx, w.nbytes)
+    d.upload(w)
+    outs = [(np.empty(dc.proof_size(256), np.uint8), np.empty((3, 256), np.uint32)) for _ in range(2)]
+    jobs = [ctx.submit(dc, None, pb, cb, d_input=d.ptr, marker=k) for k, (pb, cb) in enumerate(outs)]
+    for job, (pb, cb) in zip(jobs, outs):
+        n = ctx.wait(job)
+        assert sha(pb[:n].tobytes()) == GOLDEN["lanes256"]["proof_sha256"]
+    assert ctx.elapsed_ms(0, 1) >= 0.0
