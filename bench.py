@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--depth", type=int, default=3, help="proofs in flight (host hashing overlaps device work)")
+    ap.add_argument("--tile", default="", help="threads_per_row,block,ctas for every kernel (default: library's)")
     return ap.parse_args()
 
 
@@ -274,6 +275,8 @@ def run_ours(args, D):
     circ, widths, cfg = workload(args)
     N = args.copies
     ctx = Context(device)
+    if args.tile:
+        ctx.set_tile(*[int(x) for x in args.tile.split(",")])
     dc = ctx.load(circ)
     rows = 1 << circ.log_input_size
     plen = dc.proof_size(N)

@@ -14,6 +14,10 @@
 //   k_round        receive_challenge + poly_eval_at(k)        sumcheck_helper.hpp:104-133, 68-102
 //   k_s_build      _prepare_h_y_vals (copy-independent part)  sumcheck_helper.hpp:233-261
 //   k_wsum         eval_multilinear via an eq table           include/poly_commit/poly.hpp:88-104
+//
+// The per-repetition kernels (k_hg_round0, k_round) give each CTA one repetition j =
+// blockIdx.x % R: the R CTAs of a row chunk are adjacent in launch order, run together and
+// share the layer input through L2, while each thread keeps only one repetition's state.
 #include "kernels.cuh"
 #include "m31.cuh"
 
@@ -47,13 +51,21 @@ __device__ __forceinline__ uint32_t reduce64(unsigned long long x) {
     return m31::umin(s, s - m31::P);
 }
 
-// Block reduction of C components x 4 lanes per thread over the CTA's row slices, one
-// 64-bit atomic add per (component, lane) into red.acc, then the last CTA to arrive
-// turns the totals into canonical values, hands them to fin(lane, vals[C]) and re-zeroes
-// the scratch for the next launch.
+// Canonical total of component c at `lane`, re-zeroing the accumulator for the next launch.
+__device__ __forceinline__ uint32_t take(const RedScratch& red, uint32_t c, uint32_t N, uint32_t lane) {
+    unsigned long long* p = &red.acc[(size_t)c * N + lane];
+    const uint32_t v = reduce64(__ldcg(p));
+    *p = 0ull;
+    return v;
+}
+
+// Reduction of C components x 4 lanes per thread: a shared-memory reduction over the CTA's
+// row slices, one 64-bit atomic add per (component, lane) into red.acc at component
+// comp_base + c, then the last CTA of this lane group (ticket blockIdx.y) hands every lane
+// of the group to fin(lane), which collects the totals with take().
 template <int C, class Fin>
-__device__ __forceinline__ void reduce_epilogue(const uint32_t (&acc)[C][4], const Geo& g, bool active, RedScratch red,
-                                                Fin fin) {
+__device__ __forceinline__ void reduce_group(const uint32_t (&acc)[C][4], const Geo& g, bool active, RedScratch red,
+                                             uint32_t comp_base, Fin fin) {
     extern __shared__ uint32_t smem[];
     const uint32_t tid = threadIdx.x, B = blockDim.x;
 #pragma unroll
@@ -69,26 +81,18 @@ __device__ __forceinline__ void reduce_epilogue(const uint32_t (&acc)[C][4], con
         for (uint32_t r = 0; r < rps; r++) s += col[r * tpr];
         const uint32_t c = cl >> 2, l = cl & 3;
         const uint32_t lane = (blockIdx.y * tpr + q) * 4 + l;
-        atomicAdd(&red.acc[(size_t)c * g.N + lane], s);
+        atomicAdd(&red.acc[(size_t)(comp_base + c) * g.N + lane], s);
     }
     __threadfence();
     __syncthreads();
     __shared__ unsigned int is_last;
-    if (tid == 0) is_last = (atomicAdd(red.ticket, 1u) == gridDim.x * gridDim.y - 1) ? 1u : 0u;
+    if (tid == 0) is_last = (atomicAdd(&red.ticket[blockIdx.y], 1u) == gridDim.x - 1) ? 1u : 0u;
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    for (uint32_t lane = tid; lane < g.N; lane += B) {
-        uint32_t v[C];
-#pragma unroll
-        for (int c = 0; c < C; c++) {
-            unsigned long long* p = &red.acc[(size_t)c * g.N + lane];
-            v[c] = reduce64(__ldcg(p));
-            *p = 0ull;
-        }
-        fin(lane, v);
-    }
-    if (tid == 0) *red.ticket = 0u;
+    const uint32_t lanes = 4 * tpr, base = blockIdx.y * lanes;
+    for (uint32_t li = tid; li < lanes; li += B) fin(base + li);
+    if (tid == 0) red.ticket[blockIdx.y] = 0u;
 }
 
 struct TileIdx {
@@ -192,17 +196,18 @@ __global__ void k_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* _
     }
 }
 
-// ---------------------------------------------------------------- round finishers
-template <int R>
+// ---------------------------------------------------------------- finishers
+// Evaluations at 0, 1, 2 of every repetition's round polynomial for one lane; with vx the
+// phase-two sums are multiplied by v(rx) (h = v(rx) * s).
 struct RoundFin {
-    uint32_t* out;       // R x 3 x N: evaluations at 0, 1, 2 per repetition
-    const uint32_t* vx;  // R x N phase-two factor v(rx), or null
-    uint32_t N;
-    __device__ void operator()(uint32_t lane, const uint32_t* v) const {
-#pragma unroll
-        for (int j = 0; j < R; j++) {
-            uint32_t p0 = v[3 * j], p1 = v[3 * j + 1];
-            uint32_t p2 = m31::eval_at_two(p0, p1, v[3 * j + 2]);
+    RedScratch red;
+    uint32_t* out;       // R x 3 x N
+    const uint32_t* vx;  // R x N, or null
+    uint32_t N, reps;
+    __device__ void operator()(uint32_t lane) const {
+        for (uint32_t j = 0; j < reps; j++) {
+            uint32_t p0 = take(red, 3 * j, N, lane), p1 = take(red, 3 * j + 1, N, lane);
+            uint32_t p2 = m31::eval_at_two(p0, p1, take(red, 3 * j + 2, N, lane));
             if (vx) {
                 const uint32_t x = vx[(size_t)j * N + lane];
                 p0 = mul(p0, x); p1 = mul(p1, x); p2 = mul(p2, x);
@@ -214,42 +219,37 @@ struct RoundFin {
     }
 };
 
-template <int R>
 struct CopyFin {
-    uint32_t* out;  // R x N
-    uint32_t N;
-    __device__ void operator()(uint32_t lane, const uint32_t* v) const {
-#pragma unroll
-        for (int j = 0; j < R; j++) out[(size_t)j * N + lane] = v[j];
+    RedScratch red;
+    uint32_t* out;  // reps x N
+    uint32_t N, reps;
+    __device__ void operator()(uint32_t lane) const {
+        for (uint32_t j = 0; j < reps; j++) out[(size_t)j * N + lane] = take(red, j, N, lane);
     }
 };
 
-template <int R>
-__device__ __forceinline__ void accum_pair(uint32_t (&acc)[3 * R][4], int j, const uint32_t (&f0)[4],
-                                           const uint32_t (&f1)[4], const uint32_t (&h0)[4], const uint32_t (&h1)[4]) {
+__device__ __forceinline__ void accum_pair(uint32_t (&acc)[3][4], const uint32_t (&f0)[4], const uint32_t (&f1)[4],
+                                           const uint32_t (&h0)[4], const uint32_t (&h1)[4]) {
 #pragma unroll
     for (int l = 0; l < 4; l++) {
-        acc[3 * j][l] = add(acc[3 * j][l], mul(f0[l], h0[l]));
-        acc[3 * j + 1][l] = add(acc[3 * j + 1][l], mul(f1[l], h1[l]));
-        acc[3 * j + 2][l] = add(acc[3 * j + 2][l], mul(add(f0[l], f1[l]), add(h0[l], h1[l])));
+        acc[0][l] = add(acc[0][l], mul(f0[l], h0[l]));
+        acc[1][l] = add(acc[1][l], mul(f1[l], h1[l]));
+        acc[2][l] = add(acc[2][l], mul(add(f0[l], f1[l]), add(h0[l], h1[l])));
     }
 }
 
 // ---------------------------------------------------------------- phase one: hg build + round 0
 // For each pair (x0, x1) = (2i, 2i+1): hg_j[x] = a_j[x] + sum over mul gates (x, y, k) of
 // v[y] * w_j[k], written for the later folds, then the round-0 sums of v(x) hg_j(x).
+// All repetitions in one thread: each gathered v[y] row serves the R weights.
 template <int R>
-__global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ v, uint64_t I,
-                                                   const uint32_t* __restrict__ mx_off, const uint4* __restrict__ mx_g,
-                                                   const uint4* __restrict__ a4, const uint4* __restrict__ w4,
-                                                   uint32_t* hg0, uint32_t* hg1, uint32_t* hg2, Geo g, RedScratch red,
-                                                   uint32_t* evals_out) {
+__global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict__ v, uint64_t I,
+                                                      const uint32_t* __restrict__ mx_off, const uint4* __restrict__ mx_g,
+                                                      const uint4* __restrict__ a4, const uint4* __restrict__ w4,
+                                                      uint32_t* hg0, uint32_t* hg1, uint32_t* hg2, Geo g,
+                                                      RedScratch red, uint32_t* evals_out) {
     const TileIdx t = tile_idx(g);
-    uint32_t acc[3 * R][4];
-#pragma unroll
-    for (int c = 0; c < 3 * R; c++)
-#pragma unroll
-        for (int l = 0; l < 4; l++) acc[c][l] = 0u;
+    uint32_t acc[3 * R][4] = {};
     uint32_t* hg[3] = {hg0, hg1, hg2};
     if (t.active) {
         const uint64_t npairs = I >> 1;
@@ -277,12 +277,18 @@ __global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ 
                 for (int j = 0; j < R; j++) st4(hg[j], x, g.N, t.lane0, mk4(h[s][j]));
             }
             const uint4 v0 = ld4(v, 2 * i, g.N, t.lane0), v1 = ld4(v, 2 * i + 1, g.N, t.lane0);
-            const uint32_t f0[4] = {v0.x, v0.y, v0.z, v0.w}, f1[4] = {v1.x, v1.y, v1.z, v1.w};
 #pragma unroll
-            for (int j = 0; j < R; j++) accum_pair<R>(acc, j, f0, f1, h[0][j], h[1][j]);
+            for (int j = 0; j < R; j++)
+#pragma unroll
+                for (int l = 0; l < 4; l++) {
+                    const uint32_t f0 = comp(v0, l), f1 = comp(v1, l);
+                    acc[3 * j][l] = add(acc[3 * j][l], mul(f0, h[0][j][l]));
+                    acc[3 * j + 1][l] = add(acc[3 * j + 1][l], mul(f1, h[1][j][l]));
+                    acc[3 * j + 2][l] = add(acc[3 * j + 2][l], mul(add(f0, f1), add(h[0][j][l], h[1][j][l])));
+                }
         }
     }
-    reduce_epilogue<3 * R>(acc, g, t.active, red, RoundFin<R>{evals_out, nullptr, g.N});
+    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R});
 }
 
 // ---------------------------------------------------------------- fold + reduce round
@@ -293,86 +299,68 @@ __global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ 
 // SHARED: every repetition folds the same source table (the layer input at round 1).
 // LANE_HG: hg is a per-copy table (phase one); otherwise it is a copy-independent scalar
 // table s_j (phase two) and the finisher multiplies the sums by vx_j.
-template <int R, bool SHARED, bool LANE_HG, bool FOLD>
+template <bool SHARED, bool LANE_HG, bool FOLD>
 __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx, Geo g,
-                                               RedScratch red, uint32_t* evals_out) {
+                                               uint32_t reps, RedScratch red, uint32_t* evals_out) {
     const TileIdx t = tile_idx(g);
-    uint32_t acc[3 * R][4];
-#pragma unroll
-    for (int c = 0; c < 3 * R; c++)
-#pragma unroll
-        for (int l = 0; l < 4; l++) acc[c][l] = 0u;
+    const uint32_t j = blockIdx.x % reps, cx = blockIdx.x / reps, nx = gridDim.x / reps;
+    // selects instead of p.x[j]: a dynamic index into kernel parameters would copy them to the stack
+    const uint32_t* __restrict__ fs = (SHARED || j == 0) ? p.fsrc[0] : (j == 1 ? p.fsrc[1] : p.fsrc[2]);
+    const uint32_t* __restrict__ hs = j == 0 ? p.hsrc[0] : (j == 1 ? p.hsrc[1] : p.hsrc[2]);
+    uint32_t* __restrict__ fd = j == 0 ? p.fdst[0] : (j == 1 ? p.fdst[1] : p.fdst[2]);
+    uint32_t* __restrict__ hd = j == 0 ? p.hdst[0] : (j == 1 ? p.hdst[1] : p.hdst[2]);
+    const uint32_t r = j == 0 ? p.r[0] : (j == 1 ? p.r[1] : p.r[2]);
+    uint32_t acc[3][4] = {};
     if (t.active) {
-        for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
-            uint4 sh[4];
-            if (SHARED) {
-                if (FOLD) {
+        for (uint64_t i = (uint64_t)cx * g.rps + t.rs; i < npairs; i += (uint64_t)nx * g.rps) {
+            uint32_t f0[4], f1[4], h0[4], h1[4];
+            if (FOLD) {
+                uint4 a[4];
 #pragma unroll
-                    for (int k = 0; k < 4; k++) sh[k] = ld4(p.fsrc[0], 4 * i + k, g.N, t.lane0);
-                } else {
-                    sh[0] = ld4(p.fsrc[0], 2 * i, g.N, t.lane0);
-                    sh[1] = ld4(p.fsrc[0], 2 * i + 1, g.N, t.lane0);
-                }
-            }
+                for (int k = 0; k < 4; k++) a[k] = ld4(fs, 4 * i + k, g.N, t.lane0);
+                if (LANE_HG) {
+                    uint4 b[4];
 #pragma unroll
-            for (int j = 0; j < R; j++) {
-                uint32_t f0[4], f1[4], h0[4], h1[4];
-                const uint32_t r = p.r[j];
-                if (FOLD) {
-                    uint4 a[4];
-#pragma unroll
-                    for (int k = 0; k < 4; k++) a[k] = SHARED ? sh[k] : ld4(p.fsrc[j], 4 * i + k, g.N, t.lane0);
+                    for (int k = 0; k < 4; k++) b[k] = ld4(hs, 4 * i + k, g.N, t.lane0);
 #pragma unroll
                     for (int l = 0; l < 4; l++) {
-                        f0[l] = fold(comp(a[0], l), comp(a[1], l), r);
-                        f1[l] = fold(comp(a[2], l), comp(a[3], l), r);
+                        h0[l] = fold(comp(b[0], l), comp(b[1], l), r);
+                        h1[l] = fold(comp(b[2], l), comp(b[3], l), r);
                     }
-                    st4(p.fdst[j], 2 * i, g.N, t.lane0, mk4(f0));
-                    st4(p.fdst[j], 2 * i + 1, g.N, t.lane0, mk4(f1));
+                    st4(hd, 2 * i, g.N, t.lane0, mk4(h0));
+                    st4(hd, 2 * i + 1, g.N, t.lane0, mk4(h1));
                 } else {
-                    const uint4 a0 = SHARED ? sh[0] : ld4(p.fsrc[j], 2 * i, g.N, t.lane0);
-                    const uint4 a1 = SHARED ? sh[1] : ld4(p.fsrc[j], 2 * i + 1, g.N, t.lane0);
-#pragma unroll
-                    for (int l = 0; l < 4; l++) { f0[l] = comp(a0, l); f1[l] = comp(a1, l); }
-                }
-                if (LANE_HG) {
-                    if (FOLD) {
-                        uint4 b[4];
-#pragma unroll
-                        for (int k = 0; k < 4; k++) b[k] = ld4(p.hsrc[j], 4 * i + k, g.N, t.lane0);
-#pragma unroll
-                        for (int l = 0; l < 4; l++) {
-                            h0[l] = fold(comp(b[0], l), comp(b[1], l), r);
-                            h1[l] = fold(comp(b[2], l), comp(b[3], l), r);
-                        }
-                        st4(p.hdst[j], 2 * i, g.N, t.lane0, mk4(h0));
-                        st4(p.hdst[j], 2 * i + 1, g.N, t.lane0, mk4(h1));
-                    } else {
-                        const uint4 b0 = ld4(p.hsrc[j], 2 * i, g.N, t.lane0), b1 = ld4(p.hsrc[j], 2 * i + 1, g.N, t.lane0);
-#pragma unroll
-                        for (int l = 0; l < 4; l++) { h0[l] = comp(b0, l); h1[l] = comp(b1, l); }
-                    }
-                } else {
-                    uint32_t s0, s1;
-                    if (FOLD) {
-                        const uint4 s = __ldg(reinterpret_cast<const uint4*>(p.hsrc[j]) + i);
-                        s0 = fold(s.x, s.y, r);
-                        s1 = fold(s.z, s.w, r);
-                        if (t.q == 0 && blockIdx.y == 0)
-                            *reinterpret_cast<uint2*>(p.hdst[j] + 2 * i) = make_uint2(s0, s1);
-                    } else {
-                        const uint2 s = __ldg(reinterpret_cast<const uint2*>(p.hsrc[j]) + i);
-                        s0 = s.x;
-                        s1 = s.y;
-                    }
+                    const uint4 s = __ldg(reinterpret_cast<const uint4*>(hs) + i);
+                    const uint32_t s0 = fold(s.x, s.y, r), s1 = fold(s.z, s.w, r);
+                    if (t.q == 0 && blockIdx.y == 0) *reinterpret_cast<uint2*>(hd + 2 * i) = make_uint2(s0, s1);
 #pragma unroll
                     for (int l = 0; l < 4; l++) { h0[l] = s0; h1[l] = s1; }
                 }
-                accum_pair<R>(acc, j, f0, f1, h0, h1);
+#pragma unroll
+                for (int l = 0; l < 4; l++) {
+                    f0[l] = fold(comp(a[0], l), comp(a[1], l), r);
+                    f1[l] = fold(comp(a[2], l), comp(a[3], l), r);
+                }
+                st4(fd, 2 * i, g.N, t.lane0, mk4(f0));
+                st4(fd, 2 * i + 1, g.N, t.lane0, mk4(f1));
+            } else {
+                const uint4 a0 = ld4(fs, 2 * i, g.N, t.lane0), a1 = ld4(fs, 2 * i + 1, g.N, t.lane0);
+#pragma unroll
+                for (int l = 0; l < 4; l++) { f0[l] = comp(a0, l); f1[l] = comp(a1, l); }
+                if (LANE_HG) {
+                    const uint4 b0 = ld4(hs, 2 * i, g.N, t.lane0), b1 = ld4(hs, 2 * i + 1, g.N, t.lane0);
+#pragma unroll
+                    for (int l = 0; l < 4; l++) { h0[l] = comp(b0, l); h1[l] = comp(b1, l); }
+                } else {
+                    const uint2 s = __ldg(reinterpret_cast<const uint2*>(hs) + i);
+#pragma unroll
+                    for (int l = 0; l < 4; l++) { h0[l] = s.x; h1[l] = s.y; }
+                }
             }
+            accum_pair(acc, f0, f1, h0, h1);
         }
     }
-    reduce_epilogue<3 * R>(acc, g, t.active, red, RoundFin<R>{evals_out, LANE_HG ? nullptr : vx, g.N});
+    reduce_group<3>(acc, g, t.active, red, 3 * j, RoundFin{red, evals_out, LANE_HG ? nullptr : vx, g.N, reps});
 }
 
 // ---------------------------------------------------------------- phase two: s(y)
@@ -419,7 +407,7 @@ __global__ void __launch_bounds__(256) k_wsum(const uint32_t* __restrict__ vals,
             }
         }
     }
-    reduce_epilogue<R>(acc, g, t.active, red, CopyFin<R>{out, g.N});
+    reduce_group<R>(acc, g, t.active, red, 0, CopyFin{red, out, g.N, (uint32_t)R});
 }
 
 uint32_t grid_1d(uint64_t n, uint32_t block) {
@@ -427,6 +415,13 @@ uint32_t grid_1d(uint64_t n, uint32_t block) {
     if (b < 1) b = 1;
     if (b > 152ull * 16) b = 152ull * 16;
     return (uint32_t)b;
+}
+
+// Row tile with repetition-split CTAs: gridDim.x = reps x row chunks.
+LaunchShape rep_shape(const Geo& g, uint64_t rows, uint32_t block, uint32_t ctas_cap, uint32_t reps) {
+    LaunchShape s = row_shape(g, rows, block, ctas_cap / reps, 3);
+    s.grid.x *= reps;
+    return s;
 }
 
 }  // namespace
@@ -482,11 +477,14 @@ cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint
     return cudaGetLastError();
 }
 
-template <int R>
-static void round_dispatch(bool shared_src, bool lane_hg, bool fold_, const LaunchShape& sh, cudaStream_t s,
-                           const RoundPtrs& p, uint64_t npairs, const uint32_t* vx, const Geo& g, RedScratch red,
-                           uint32_t* ev) {
-#define GKR_ROUND(SH, LH, FO) k_round<R, SH, LH, FO><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, ev)
+cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, const RoundPtrs& p, uint64_t npairs,
+                         const uint32_t* vx, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
+                         uint32_t* evals_out, cudaStream_t s) {
+    if (reps < 1 || reps > 3) return cudaErrorInvalidValue;
+    if (lane_hg && !fold_) return cudaErrorInvalidValue;  // phase-one round 0 lives in k_hg_round0
+    if (!fold_ && !shared_src) return cudaErrorInvalidValue;
+    LaunchShape sh = rep_shape(g, npairs, block, ctas, reps);
+#define GKR_ROUND(SH, LH, FO) k_round<SH, LH, FO><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, reps, red, evals_out)
     if (lane_hg) {
         if (shared_src) GKR_ROUND(true, true, true);
         else GKR_ROUND(false, true, true);
@@ -497,20 +495,6 @@ static void round_dispatch(bool shared_src, bool lane_hg, bool fold_, const Laun
         GKR_ROUND(true, false, false);
     }
 #undef GKR_ROUND
-}
-
-cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, const RoundPtrs& p, uint64_t npairs,
-                         const uint32_t* vx, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
-                         uint32_t* evals_out, cudaStream_t s) {
-    if (lane_hg && !fold_) return cudaErrorInvalidValue;  // phase-one round 0 lives in k_hg_round0
-    if (!fold_ && !shared_src) return cudaErrorInvalidValue;
-    LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
-    switch (reps) {
-        case 1: round_dispatch<1>(shared_src, lane_hg, fold_, sh, s, p, npairs, vx, g, red, evals_out); break;
-        case 2: round_dispatch<2>(shared_src, lane_hg, fold_, sh, s, p, npairs, vx, g, red, evals_out); break;
-        case 3: round_dispatch<3>(shared_src, lane_hg, fold_, sh, s, p, npairs, vx, g, red, evals_out); break;
-        default: return cudaErrorInvalidValue;
-    }
     return cudaGetLastError();
 }
 

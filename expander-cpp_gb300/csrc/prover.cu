@@ -2,27 +2,34 @@
 //
 // Prove flow, following Prover::prove (include/LinearGKR/LinearGKR.hpp:58-90) and
 // gkr_prove (include/LinearGKR/gkr.hpp:24-73):
+//   host   : RAW commitment bytes -> transcript, grinding (a host worker, overlapped)
 //   device : input -> Circuit::evaluate of every layer, kept resident for the sumcheck
-//   host   : RAW commitment bytes -> transcript, grinding, output challenges rz1
 //   device : claimed_v = eval_multilinear(output, rz1_j) for every repetition j
 //   per layer, top down, per sumcheck_prove_gkr_layer (include/LinearGKR/sumcheck.hpp:52-111):
 //     device : eq tables, gate weights, hg build fused with round 0
-//     rounds : device fold+reduce for all repetitions at once -> 3R rows to the host ->
-//              host appends them and derives the R challenges in the reference's order
+//     rounds : device fold+reduce for all repetitions -> 3R rows to the host -> the host
+//              appends them and derives the R challenges in the reference's order
 //     phase 2: s(y) table, rounds over the layer input with h = v(rx) * s
 //   alpha, beta challenges between layers.
 // The host does only transcript work: appending bytes, SHA-256, and the last 2->1 fold of
 // each phase's table (vx, vy: 2 rows x N lanes), whose result must enter the transcript
 // before the next repetition's challenge.
+//
+// Concurrency: a context owns `lanes` device workers, each with its own stream, so the
+// device stages of several proofs overlap (continuous batching: a queued proof starts as
+// soon as a lane is free and its device workspace fits in the HBM budget).  Each proof's
+// workspace is one block from a stream-ordered memory pool, returned when the proof ends.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <stdexcept>
@@ -88,15 +95,12 @@ int reps_for(int grinding_bits) {
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-struct DevBuf {
+// Pinned host buffer that grows on demand.
+struct PinnedBuf {
     void* p = nullptr;
     size_t cap = 0;
-    bool pinned = false;
     void release() {
-        if (p) {
-            if (pinned) cudaFreeHost(p);
-            else cudaFree(p);
-        }
+        if (p) cudaFreeHost(p);
         p = nullptr;
         cap = 0;
     }
@@ -106,11 +110,11 @@ struct DevBuf {
         bytes = std::max<size_t>(align_up(bytes, 256), 256);
         if (bytes <= cap) return;
         release();
-        cudaError_t e = pinned ? cudaMallocHost(&p, bytes) : cudaMalloc(&p, bytes);
+        cudaError_t e = cudaMallocHost(&p, bytes);
         if (e != cudaSuccess) {
             p = nullptr;
             cudaGetLastError();
-            fail(GKRGPU_ERR_NOMEM, "allocation of %zu bytes for %s failed: %s", bytes, what, cudaGetErrorString(e));
+            fail(GKRGPU_ERR_NOMEM, "pinned allocation of %zu bytes for %s failed: %s", bytes, what, cudaGetErrorString(e));
         }
         cap = bytes;
     }
@@ -188,20 +192,90 @@ struct gkrgpu_job {
     std::condition_variable cv;
 };
 
+// ------------------------------------------------------------------ lanes
+// One device worker's state: its stream, pinned staging buffers, launch accounting.
+struct Lane {
+    gkrgpu_ctx* X = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done_ev = nullptr;
+    PinnedBuf h_evals, h_rows, h_vx, h_cv, h_flag;
+
+    struct Rec {
+        int kid;
+        size_t e0, e1;
+    };
+    std::vector<cudaEvent_t> events;
+    size_t ev_used = 0;
+    std::vector<Rec> recs;
+    uint64_t job_launches[K_NUM_KERNELS] = {};
+    double job_bytes[K_NUM_KERNELS] = {};
+
+    ~Lane() {
+        for (PinnedBuf* b : {&h_evals, &h_rows, &h_vx, &h_cv, &h_flag}) b->release();
+        for (auto e : events) cudaEventDestroy(e);
+        if (done_ev) cudaEventDestroy(done_ev);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    size_t next_event() {
+        if (ev_used == events.size()) {
+            cudaEvent_t e;
+            ck(cudaEventCreate(&e), "cudaEventCreate");
+            events.push_back(e);
+        }
+        return ev_used++;
+    }
+    template <class F>
+    void launch(int kid, double algo_bytes, F&& f);
+    void resolve_events();
+    void discard_job_stats() {
+        recs.clear();
+        ev_used = 0;
+        for (int k = 0; k < K_NUM_KERNELS; k++) {
+            job_launches[k] = 0;
+            job_bytes[k] = 0;
+        }
+    }
+    // Waits for the stream: short spin, then yields the core (many lanes may be waiting).
+    void sync() {
+        ck(cudaEventRecord(done_ev, stream), "cudaEventRecord");
+        const auto t0 = std::chrono::steady_clock::now();
+        for (;;) {
+            const cudaError_t e = cudaEventQuery(done_ev);
+            if (e == cudaSuccess) return;
+            if (e != cudaErrorNotReady) ck(e, "cudaEventQuery");
+            if (std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(50)) std::this_thread::yield();
+        }
+    }
+    void copy(void* dst, const void* src, size_t n, cudaMemcpyKind kind, const char* what);
+};
+
 // ------------------------------------------------------------------ context
 struct gkrgpu_ctx {
     int device = 0;
     int sm_count = 152;
-    cudaStream_t stream = nullptr;
-    uint32_t tpr_max = 32, block = 256, ctas = 0;
+    // Row tile per kernel kind: threads per row slice (4 copies each) and CTA budget
+    // (0 = the kind's default); chosen by gkrgpu_autotune or set with gkrgpu_set_tile.
+    struct Tile {
+        uint32_t tpr = 32, ctas = 0;
+    };
+    Tile tiles[K_NUM_KERNELS];
+    uint32_t block = 256;
 
-    // job pipeline: one device-stage worker, host-stage workers
+    // device memory: per-proof workspaces from a stream-ordered pool, admitted by budget
+    cudaMemPool_t pool = nullptr;
+    uint64_t hbm_budget = 0, hbm_in_use = 0, hbm_peak = 0;
+    std::mutex mem_m;
+    std::condition_variable mem_cv;
+
+    // job pipeline: `n_lanes` device-stage workers, host-stage workers
     std::mutex qm;
     std::condition_variable qcv;
     std::deque<gkrgpu_job*> host_q, gpu_q;
     std::vector<std::thread> workers;
-    bool stopping = false, gpu_busy = false;
-    int host_workers = 2;
+    std::vector<std::unique_ptr<Lane>> lanes;
+    int n_lanes = 1, host_workers = 2, running = 0;
+    bool stopping = false;
+
     void start_workers();
     void shutdown() {
         {
@@ -215,117 +289,43 @@ struct gkrgpu_ctx {
     // Waits until no device stage is queued or running.
     void drain() {
         std::unique_lock<std::mutex> lk(qm);
-        qcv.wait(lk, [&] { return gpu_q.empty() && !gpu_busy; });
+        qcv.wait(lk, [&] { return gpu_q.empty() && running == 0; });
+    }
+    Lane& lane(int i) {
+        while ((int)lanes.size() <= i) {
+            auto L = std::make_unique<Lane>();
+            L->X = this;
+            ck(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            ck(cudaEventCreateWithFlags(&L->done_ev, cudaEventDisableTiming), "cudaEventCreate");
+            lanes.push_back(std::move(L));
+        }
+        return *lanes[i];
     }
 
-    DevBuf vals, eqc, eqrx, a4, w4, acc, ticket, evals, vx, cv, flag;
-    DevBuf fA[3], fB[3], hg0[3], hgA[3], sb[2];
-    DevBuf h_evals, h_rows, h_vx, h_cv, h_flag;  // pinned
-
-    // launch accounting
+    // launch accounting: totals read under stats_m; lanes fold each finished job in
     bool timing = false;
     std::atomic<uint64_t> h2d_bytes{0}, d2h_bytes{0};
     cudaEvent_t markers[64] = {};
-    // Totals (read by gkrgpu_kernel_stats under stats_m); each job's launches accumulate
-    // in job_* and are folded in when the job ends, so snapshots fall on job boundaries.
     std::mutex stats_m;
     uint64_t launches[K_NUM_KERNELS] = {};
     double ms[K_NUM_KERNELS] = {};
     double bytes[K_NUM_KERNELS] = {};
-    uint64_t job_launches[K_NUM_KERNELS] = {};
-    double job_bytes[K_NUM_KERNELS] = {};
-    struct Rec {
-        int kid;
-        size_t e0, e1;
-    };
-    std::vector<cudaEvent_t> events;
-    size_t ev_used = 0;
-    std::vector<Rec> recs;
 
-    gkrgpu_ctx() {
-        for (DevBuf* b : {&h_evals, &h_rows, &h_vx, &h_cv, &h_flag}) b->pinned = true;
-    }
     ~gkrgpu_ctx() {
         DeviceGuard g(device);
-        for (DevBuf* b : {&vals, &eqc, &eqrx, &a4, &w4, &acc, &ticket, &evals, &vx, &cv, &flag, &h_evals, &h_rows,
-                          &h_vx, &h_cv, &h_flag})
-            b->release();
-        for (int j = 0; j < 3; j++) {
-            fA[j].release(); fB[j].release(); hg0[j].release(); hgA[j].release();
-        }
-        sb[0].release(); sb[1].release();
-        for (auto e : events) cudaEventDestroy(e);
+        lanes.clear();
         for (auto e : markers)
             if (e) cudaEventDestroy(e);
-        if (stream) cudaStreamDestroy(stream);
+        if (pool) cudaMemPoolDestroy(pool);
     }
 
-    size_t next_event() {
-        if (ev_used == events.size()) {
-            cudaEvent_t e;
-            ck(cudaEventCreate(&e), "cudaEventCreate");
-            events.push_back(e);
-        }
-        return ev_used++;
-    }
-    // Brackets one launch: f() enqueues the kernel on `stream`.
-    template <class F>
-    void launch(int kid, double algo_bytes, F&& f) {
-        size_t e0 = 0;
-        if (timing) {
-            e0 = next_event();
-            ck(cudaEventRecord(events[e0], stream), "cudaEventRecord");
-        }
-        ck(f(), kKernelNames[kid]);
-        job_launches[kid]++;
-        job_bytes[kid] += algo_bytes;
-        if (timing) {
-            const size_t e1 = next_event();
-            ck(cudaEventRecord(events[e1], stream), "cudaEventRecord");
-            recs.push_back({kid, e0, e1});
-        }
-    }
-    // Folds the finished job's launch counts, bytes and event times into the totals; the
-    // stream must be idle.
-    void resolve_events() {
-        double t_ms[K_NUM_KERNELS] = {};
-        for (const Rec& r : recs) {
-            float t = 0.f;
-            ck(cudaEventElapsedTime(&t, events[r.e0], events[r.e1]), "cudaEventElapsedTime");
-            t_ms[r.kid] += t;
-        }
-        recs.clear();
-        ev_used = 0;
-        std::lock_guard<std::mutex> lk(stats_m);
-        for (int k = 0; k < K_NUM_KERNELS; k++) {
-            launches[k] += job_launches[k];
-            bytes[k] += job_bytes[k];
-            ms[k] += t_ms[k];
-            job_launches[k] = 0;
-            job_bytes[k] = 0;
-        }
-    }
-    void discard_job_stats() {
-        recs.clear();
-        ev_used = 0;
-        for (int k = 0; k < K_NUM_KERNELS; k++) {
-            job_launches[k] = 0;
-            job_bytes[k] = 0;
-        }
-    }
-    void sync() { ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
-    // Stream-ordered copy, counted in the transfer statistics.
-    void copy(void* dst, const void* src, size_t n, cudaMemcpyKind kind, const char* what) {
-        ck(cudaMemcpyAsync(dst, src, n, kind, stream), what);
-        if (kind == cudaMemcpyHostToDevice) h2d_bytes += n;
-        if (kind == cudaMemcpyDeviceToHost) d2h_bytes += n;
-    }
-
-    Geo geo(uint32_t N) const {
+    // Tile of kernel kind `kid` for N copies: the largest divisor of N/4 not above its tpr.
+    Geo geo(uint32_t N, int kid) const {
         const uint32_t Q = N / 4;
         uint32_t tpr = Q;
-        if (tpr > tpr_max) {
-            tpr = tpr_max;
+        const uint32_t want = std::min<uint32_t>(tiles[kid].tpr, block);
+        if (tpr > want) {
+            tpr = want;
             while (tpr > 1 && Q % tpr) tpr--;
         }
         Geo g;
@@ -334,9 +334,70 @@ struct gkrgpu_ctx {
         g.rps = block / tpr;
         return g;
     }
-    uint32_t cta_budget() const { return ctas ? ctas : (uint32_t)sm_count * 4; }
-    RedScratch red() const { return RedScratch{acc.as<unsigned long long>(), ticket.as<unsigned int>()}; }
+    uint32_t cta_budget(int kid) const {
+        if (tiles[kid].ctas) return tiles[kid].ctas;
+        return (uint32_t)sm_count * (kid == K_EVALUATE ? 16u : 4u);
+    }
+
+    // Blocks until `bytes` fit in the budget (a proof larger than the whole budget runs alone).
+    void acquire_hbm(uint64_t bytes) {
+        std::unique_lock<std::mutex> lk(mem_m);
+        mem_cv.wait(lk, [&] { return hbm_in_use == 0 || hbm_in_use + bytes <= hbm_budget; });
+        hbm_in_use += bytes;
+        hbm_peak = std::max(hbm_peak, hbm_in_use);
+    }
+    void release_hbm(uint64_t bytes) {
+        {
+            std::lock_guard<std::mutex> lk(mem_m);
+            hbm_in_use -= bytes;
+        }
+        mem_cv.notify_all();
+    }
 };
+
+template <class F>
+void Lane::launch(int kid, double algo_bytes, F&& f) {
+    size_t e0 = 0;
+    if (X->timing) {
+        e0 = next_event();
+        ck(cudaEventRecord(events[e0], stream), "cudaEventRecord");
+    }
+    ck(f(), kKernelNames[kid]);
+    job_launches[kid]++;
+    job_bytes[kid] += algo_bytes;
+    if (X->timing) {
+        const size_t e1 = next_event();
+        ck(cudaEventRecord(events[e1], stream), "cudaEventRecord");
+        recs.push_back({kid, e0, e1});
+    }
+}
+
+// Folds the finished job's launch counts, bytes and event times into the context's totals;
+// the stream must be idle.
+void Lane::resolve_events() {
+    double t_ms[K_NUM_KERNELS] = {};
+    for (const Rec& r : recs) {
+        float t = 0.f;
+        ck(cudaEventElapsedTime(&t, events[r.e0], events[r.e1]), "cudaEventElapsedTime");
+        t_ms[r.kid] += t;
+    }
+    recs.clear();
+    ev_used = 0;
+    std::lock_guard<std::mutex> lk(X->stats_m);
+    for (int k = 0; k < K_NUM_KERNELS; k++) {
+        X->launches[k] += job_launches[k];
+        X->bytes[k] += job_bytes[k];
+        X->ms[k] += t_ms[k];
+        job_launches[k] = 0;
+        job_bytes[k] = 0;
+    }
+}
+
+void Lane::copy(void* dst, const void* src, size_t n, cudaMemcpyKind kind, const char* what) {
+    ck(cudaMemcpyAsync(dst, src, n, kind, stream), what);
+    if (kind == cudaMemcpyHostToDevice) X->h2d_bytes += n;
+    if (kind == cudaMemcpyDeviceToHost) X->d2h_bytes += n;
+}
 
 namespace {
 
@@ -455,50 +516,99 @@ void validate_layers(const gkrgpu_layer_desc* layers, int n) {
     }
 }
 
-// ------------------------------------------------------------------ prover
-struct Prover {
-    gkrgpu_ctx& c;
-    const gkrgpu_circuit& C;
-    uint32_t N;
-    int R;
-    Geo g;
-    std::vector<uint32_t*> vals;  // vals[l]: input of layer l; vals[L]: output of the last layer
+// ------------------------------------------------------------------ per-proof device workspace
+// All device tables of one proof, carved from one pool block (256-byte aligned parts).
+struct Workspace {
+    uint32_t* vals = nullptr;  // every layer's values (the input's rows excluded when it is on the device)
+    uint32_t *hg0[3] = {}, *hgA[3] = {}, *fA[3] = {}, *fB[3] = {};
+    uint32_t* sb[2] = {};
+    uint32_t *eqc = nullptr, *eqrx = nullptr, *evals = nullptr, *vx = nullptr, *cv = nullptr;
+    uint4 *a4 = nullptr, *w4 = nullptr;
+    unsigned long long* acc = nullptr;
+    unsigned int* ticket = nullptr;
+    unsigned int* flag = nullptr;
+    size_t zero_off = 0, zero_bytes = 0;  // acc + ticket + flag: zeroed at the start of a proof
+    size_t sstride = 0;
+    size_t total = 0;
 
-    Prover(gkrgpu_ctx& ctx, const gkrgpu_circuit& circ, uint32_t n, int reps)
-        : c(ctx), C(circ), N(n), R(reps), g(ctx.geo(n)) {}
-
-    void reserve(bool own_input) {
+    // Lays the parts out from `base` (null: only sizes the block).
+    void plan(char* base, const gkrgpu_circuit& C, uint32_t N, int R, bool own_input, bool sumcheck) {
+        size_t o = 0;
+        auto take = [&](size_t bytes) -> char* {
+            char* p = base ? base + o : nullptr;
+            o += align_up(std::max<size_t>(bytes, 16), 256);
+            return p;
+        };
         const uint64_t rowb = (uint64_t)N * 4;
         const uint64_t maxI = 1ull << C.max_in_vars, maxO = 1ull << C.max_out_vars;
         const uint64_t rows = C.value_rows() - (own_input ? 0 : C.in_rows(0));
-        c.vals.ensure(rows * rowb, "layer values");
-        for (int j = 0; j < R; j++) {
-            c.hg0[j].ensure(maxI * rowb, "hg table");
-            c.hgA[j].ensure(std::max<uint64_t>(maxI / 2, 1) * rowb, "hg table");
-            c.fA[j].ensure(std::max<uint64_t>(maxI / 2, 1) * rowb, "folded table");
-            c.fB[j].ensure(std::max<uint64_t>(maxI / 4, 1) * rowb, "folded table");
+        vals = (uint32_t*)take(rows * rowb);
+        if (sumcheck) {
+            for (int j = 0; j < R; j++) {
+                hg0[j] = (uint32_t*)take(maxI * rowb);
+                hgA[j] = (uint32_t*)take(std::max<uint64_t>(maxI / 2, 1) * rowb);
+                fA[j] = (uint32_t*)take(std::max<uint64_t>(maxI / 2, 1) * rowb);
+                fB[j] = (uint32_t*)take(std::max<uint64_t>(maxI / 4, 1) * rowb);
+            }
+            sstride = align_up(maxI, 64);
+            sb[0] = (uint32_t*)take(R * sstride * 4);
+            sb[1] = (uint32_t*)take(R * sstride * 4);
+            eqrx = (uint32_t*)take(R * maxI * 4);
+            a4 = (uint4*)take(maxI * 16);
+            w4 = (uint4*)take(std::max<uint64_t>(C.max_mul, 1) * 16);
         }
-        c.sb[0].ensure(R * align_up(maxI, 64) * 4, "phase-two table");
-        c.sb[1].ensure(R * align_up(maxI, 64) * 4, "phase-two table");
-        c.eqc.ensure(R * maxO * 4, "eq table");
-        c.eqrx.ensure(R * maxI * 4, "eq table");
-        c.a4.ensure(maxI * 16, "add weights");
-        c.w4.ensure(std::max<uint64_t>(C.max_mul, 1) * 16, "mul weights");
-        // The reducing kernels leave their scratch zeroed; fresh scratch is zeroed here,
-        // on the context's stream, before any kernel that uses it.
-        const size_t acc_need = 9ull * N * 8;
-        if (c.acc.cap < acc_need) {
-            c.acc.ensure(acc_need, "reduction scratch");
-            ck(cudaMemsetAsync(c.acc.p, 0, c.acc.cap, c.stream), "cudaMemsetAsync");
+        eqc = (uint32_t*)take(R * maxO * 4);
+        evals = (uint32_t*)take(9ull * N * 4);
+        vx = (uint32_t*)take(3ull * N * 4);
+        cv = (uint32_t*)take(3ull * N * 4);
+        zero_off = o;
+        acc = (unsigned long long*)take(9ull * N * 8);
+        ticket = (unsigned int*)take(4096);
+        flag = (unsigned int*)take(16);
+        zero_bytes = o - zero_off;
+        total = o;
+    }
+};
+
+uint64_t workspace_bytes(const gkrgpu_circuit& C, uint32_t N, int R, bool own_input, bool sumcheck) {
+    Workspace w;
+    w.plan(nullptr, C, N, R, own_input, sumcheck);
+    return w.total;
+}
+
+// ------------------------------------------------------------------ prover
+struct Prover {
+    gkrgpu_ctx& X;
+    Lane& c;
+    const gkrgpu_circuit& C;
+    uint32_t N;
+    int R;
+    Geo gk[K_NUM_KERNELS];
+    uint32_t ck_ctas[K_NUM_KERNELS];
+    Workspace ws;
+    char* block = nullptr;
+    std::vector<uint32_t*> vals;  // vals[l]: input of layer l; vals[L]: output of the last layer
+
+    Prover(gkrgpu_ctx& ctx, Lane& lane, const gkrgpu_circuit& circ, uint32_t n, int reps)
+        : X(ctx), c(lane), C(circ), N(n), R(reps) {
+        for (int k = 0; k < K_NUM_KERNELS; k++) {
+            gk[k] = ctx.geo(n, k);
+            ck_ctas[k] = ctx.cta_budget(k);
         }
-        if (!c.ticket.p) {
-            c.ticket.ensure(256, "ticket");
-            ck(cudaMemsetAsync(c.ticket.p, 0, c.ticket.cap, c.stream), "cudaMemsetAsync");
-        }
-        c.evals.ensure(9ull * N * 4, "round evaluations");
-        c.vx.ensure(3ull * N * 4, "vx");
-        c.cv.ensure(3ull * N * 4, "claims");
-        c.flag.ensure(4, "flag");
+    }
+    ~Prover() {
+        if (block) cudaFreeAsync(block, c.stream);
+    }
+
+    RedScratch red() const { return RedScratch{ws.acc, ws.ticket}; }
+
+    void reserve(bool own_input, bool sumcheck) {
+        ws.plan(nullptr, C, N, R, own_input, sumcheck);
+        void* p = nullptr;
+        ck(cudaMallocFromPoolAsync(&p, ws.total, X.pool, c.stream), "workspace allocation");
+        block = static_cast<char*>(p);
+        ws.plan(block, C, N, R, own_input, sumcheck);
+        ck(cudaMemsetAsync(block + ws.zero_off, 0, ws.zero_bytes, c.stream), "cudaMemsetAsync");
         c.h_evals.ensure(9ull * N * 4, "pinned evaluations");
         c.h_rows.ensure(6ull * N * 4, "pinned rows");
         c.h_vx.ensure(3ull * N * 4, "pinned vx");
@@ -516,30 +626,28 @@ struct Prover {
                 vals[0] = const_cast<uint32_t*>(d_input);
                 continue;
             }
-            vals[l] = reinterpret_cast<uint32_t*>(c.vals.as<char>() + off * rowb);
+            vals[l] = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(ws.vals) + off * rowb);
             off += (l < L) ? C.in_rows(l) : C.out_rows(L - 1);
         }
     }
 
     void check_input() {
-        ck(cudaMemsetAsync(c.flag.p, 0, 4, c.stream), "cudaMemsetAsync");
         const uint64_t n = C.in_rows(0) * N;
-        c.launch(K_CHECK, (double)n * 4, [&] { return launch_check_canonical(vals[0], n, c.flag.as<unsigned>(), c.stream); });
-        c.copy(c.h_flag.p, c.flag.p, 4, cudaMemcpyDeviceToHost, "input check readback");
+        c.launch(K_CHECK, (double)n * 4, [&] { return launch_check_canonical(vals[0], n, ws.flag, c.stream); });
+        c.copy(c.h_flag.p, ws.flag, 4, cudaMemcpyDeviceToHost, "input check readback");
     }
     void require_canonical() {
         if (*c.h_flag.as<unsigned>()) fail(GKRGPU_ERR_INVALID, "input contains a value >= 2^31 - 1");
     }
 
     void evaluate() {
-        const uint32_t ctas = c.cta_budget();
         for (size_t l = 0; l < C.layers.size(); l++) {
             const DevLayer& Ly = C.layers[l];
             const uint64_t O = 1ull << Ly.nout;
             const double b = 4.0 * N * (2.0 * Ly.nmul + Ly.nadd + O) + 16.0 * Ly.nmul + 8.0 * Ly.nadd + 8.0 * (O + 1);
             c.launch(K_EVALUATE, b, [&] {
-                return launch_evaluate(vals[l], vals[l + 1], O, Ly.mo_off, Ly.mo_g, Ly.ao_off, Ly.ao_g, g, c.block,
-                                       ctas * 4, c.stream);
+                return launch_evaluate(vals[l], vals[l + 1], O, Ly.mo_off, Ly.mo_g, Ly.ao_off, Ly.ao_g,
+                                       gk[K_EVALUATE], X.block, ck_ctas[K_EVALUATE], c.stream);
             });
         }
     }
@@ -547,7 +655,7 @@ struct Prover {
     // D2H of the 3R evaluation rows and optionally `rows_from` rows 0..1 for each repetition.
     void fetch(const uint32_t* const* rows_from, bool shared_rows) {
         const uint64_t rowb = (uint64_t)N * 4;
-        c.copy(c.h_evals.p, c.evals.p, 3ull * R * rowb, cudaMemcpyDeviceToHost, "fetch evals");
+        c.copy(c.h_evals.p, ws.evals, 3ull * R * rowb, cudaMemcpyDeviceToHost, "fetch evals");
         if (rows_from) {
             for (int j = 0; j < R; j++) {
                 const uint32_t* src = shared_rows ? rows_from[0] : rows_from[j];
@@ -598,24 +706,21 @@ struct Prover {
         const uint64_t I = 1ull << n, O = 1ull << m;
         const uint64_t rowb = (uint64_t)N * 4;
         const double rb = 4.0 * N;
-        const uint32_t ctas = c.cta_budget();
         uint32_t* v = vals[li];
         uint32_t* vxh = c.h_vx.as<uint32_t>();
         std::vector<uint32_t> vy((size_t)R * N);
 
         // phase one: eqc_j = alpha eq(rz1_j) + beta eq(rz2_j), gate weights, hg + round 0
-        eq_table(c.eqc.as<uint32_t>(), rz1, rz2, alpha, beta, m);
+        eq_table(ws.eqc, rz1, rz2, alpha, beta, m);
         const double wb = 32.0 * Ly.nmul + 20.0 * I + 8.0 * Ly.nadd + 4.0 * R * (Ly.nmul + Ly.nadd);
         c.launch(K_WEIGHTS, wb, [&] {
-            return launch_weights(I, Ly.nmul, O, c.eqc.as<uint32_t>(), Ly.mx_g, Ly.ax_off, Ly.ax_g, c.a4.as<uint4>(),
-                                  c.w4.as<uint4>(), R, c.stream);
+            return launch_weights(I, Ly.nmul, O, ws.eqc, Ly.mx_g, Ly.ax_off, Ly.ax_g, ws.a4, ws.w4, R, c.stream);
         });
-        uint32_t* hg[3] = {c.hg0[0].as<uint32_t>(), R > 1 ? c.hg0[1].as<uint32_t>() : nullptr,
-                           R > 2 ? c.hg0[2].as<uint32_t>() : nullptr};
+        uint32_t* hg[3] = {ws.hg0[0], ws.hg0[1], ws.hg0[2]};
         const double hb = rb * (I + Ly.nmul + (double)R * I) + 32.0 * Ly.nmul + 20.0 * I;
         c.launch(K_HG_ROUND0, hb, [&] {
-            return launch_hg_round0(R, v, I, Ly.mx_off, Ly.mx_g, c.a4.as<uint4>(), c.w4.as<uint4>(), hg, g, c.block,
-                                    ctas, c.red(), c.evals.as<uint32_t>(), c.stream);
+            return launch_hg_round0(R, v, I, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, hg, gk[K_HG_ROUND0], X.block,
+                                    ck_ctas[K_HG_ROUND0], red(), ws.evals, c.stream);
         });
         const uint32_t* vsrc[1] = {v};
         fetch(n == 1 ? vsrc : nullptr, true);
@@ -629,16 +734,16 @@ struct Prover {
             for (int j = 0; j < R; j++) {
                 p.fsrc[j] = cur_f[j];
                 p.hsrc[j] = cur_h[j];
-                p.fdst[j] = (k & 1) ? c.fA[j].as<uint32_t>() : c.fB[j].as<uint32_t>();
-                p.hdst[j] = (k & 1) ? c.hgA[j].as<uint32_t>() : c.hg0[j].as<uint32_t>();
+                p.fdst[j] = (k & 1) ? ws.fA[j] : ws.fB[j];
+                p.hdst[j] = (k & 1) ? ws.hgA[j] : ws.hg0[j];
                 p.r[j] = rx[j][k - 1];
             }
             const uint64_t npairs = I >> (k + 1);
             const double S = 4.0 * npairs;
             const double b = rb * ((k == 1 ? 1.0 : R) * S + R * S + R * S);
             c.launch(K_ROUND_LANE, b, [&] {
-                return launch_round(R, k == 1, true, true, p, npairs, nullptr, g, c.block, ctas, c.red(),
-                                    c.evals.as<uint32_t>(), c.stream);
+                return launch_round(R, k == 1, true, true, p, npairs, nullptr, gk[K_ROUND_LANE], X.block,
+                                    ck_ctas[K_ROUND_LANE], red(), ws.evals, c.stream);
             });
             const bool last = (k == n - 1);
             fetch(last ? p.fdst : nullptr, false);
@@ -650,22 +755,21 @@ struct Prover {
         }
 
         // phase two: h(y) = vx * s(y)
-        eq_table(c.eqrx.as<uint32_t>(), rx, nullptr, 1u, 0u, n);
-        const size_t sstride = align_up(1ull << C.max_in_vars, 64);
+        eq_table(ws.eqrx, rx, nullptr, 1u, 0u, n);
+        const size_t sstride = ws.sstride;
         c.launch(K_S_BUILD, 16.0 * Ly.nmul + 4.0 * I + 4.0 * R * I + 8.0 * R * Ly.nmul, [&] {
-            return launch_s_build(I, O, Ly.my_off, Ly.my_g, c.eqc.as<uint32_t>(), c.eqrx.as<uint32_t>(),
-                                  c.sb[0].as<uint32_t>(), sstride, R, c.stream);
+            return launch_s_build(I, O, Ly.my_off, Ly.my_g, ws.eqc, ws.eqrx, ws.sb[0], sstride, R, c.stream);
         });
-        c.copy(c.vx.p, vxh, R * rowb, cudaMemcpyHostToDevice, "vx upload");
+        c.copy(ws.vx, vxh, R * rowb, cudaMemcpyHostToDevice, "vx upload");
         {
             RoundPtrs p;
             memset(&p, 0, sizeof(p));
             p.fsrc[0] = v;
-            for (int j = 0; j < R; j++) p.hsrc[j] = c.sb[0].as<uint32_t>() + j * sstride;
+            for (int j = 0; j < R; j++) p.hsrc[j] = ws.sb[0] + j * sstride;
             const uint64_t npairs = I >> 1;
             c.launch(K_ROUND_SCALAR, rb * 2.0 * npairs + 8.0 * R * npairs, [&] {
-                return launch_round(R, true, false, false, p, npairs, c.vx.as<uint32_t>(), g, c.block, ctas, c.red(),
-                                    c.evals.as<uint32_t>(), c.stream);
+                return launch_round(R, true, false, false, p, npairs, ws.vx, gk[K_ROUND_SCALAR], X.block,
+                                    ck_ctas[K_ROUND_SCALAR], red(), ws.evals, c.stream);
             });
             fetch(n == 1 ? vsrc : nullptr, true);
             transcript_round(t, ry, 0, n == 1, false, vy.data());
@@ -677,17 +781,17 @@ struct Prover {
             const int src = (k - 1) & 1, dst = k & 1;
             for (int j = 0; j < R; j++) {
                 p.fsrc[j] = cur_f[j];
-                p.fdst[j] = (k & 1) ? c.fA[j].as<uint32_t>() : c.fB[j].as<uint32_t>();
-                p.hsrc[j] = c.sb[src].as<uint32_t>() + j * sstride;
-                p.hdst[j] = c.sb[dst].as<uint32_t>() + j * sstride;
+                p.fdst[j] = (k & 1) ? ws.fA[j] : ws.fB[j];
+                p.hsrc[j] = ws.sb[src] + j * sstride;
+                p.hdst[j] = ws.sb[dst] + j * sstride;
                 p.r[j] = ry[j][k - 1];
             }
             const uint64_t npairs = I >> (k + 1);
             const double S = 4.0 * npairs;
             const double b = rb * ((k == 1 ? 1.0 : R) * S + R * S / 2) + 6.0 * R * S;
             c.launch(K_ROUND_SCALAR, b, [&] {
-                return launch_round(R, k == 1, false, true, p, npairs, c.vx.as<uint32_t>(), g, c.block, ctas, c.red(),
-                                    c.evals.as<uint32_t>(), c.stream);
+                return launch_round(R, k == 1, false, true, p, npairs, ws.vx, gk[K_ROUND_SCALAR], X.block,
+                                    ck_ctas[K_ROUND_SCALAR], red(), ws.evals, c.stream);
             });
             const bool last = (k == n - 1);
             fetch(last ? p.fdst : nullptr, false);
@@ -697,11 +801,11 @@ struct Prover {
         for (int j = 0; j < R; j++) t.append(vy.data() + (size_t)j * N, rowb);
     }
 
-    // Device front half of a proof: input upload and check, Circuit::evaluate of every layer.
-    // Asynchronous on the context's stream; it needs no transcript.
+    // Device front half of a proof: workspace, input upload and check, Circuit::evaluate of
+    // every layer.  Asynchronous on the lane's stream; it needs no transcript.
     void device_front(const uint32_t* h_input, const uint32_t* d_input) {
         const uint64_t in_bytes = C.in_rows(0) * (uint64_t)N * 4;
-        reserve(d_input == nullptr);
+        reserve(d_input == nullptr, true);
         layout_values(d_input);
         if (h_input) c.copy(vals[0], h_input, in_bytes, cudaMemcpyHostToDevice, "input upload");
         check_input();
@@ -725,13 +829,12 @@ struct Prover {
         uint32_t alpha = 1, beta = 0;
 
         // claimed_v[j] = eval_multilinear(output, rz1[j]) = sum_z eq(rz1_j, z) out[z]
-        eq_table(c.eqc.as<uint32_t>(), rz1, nullptr, 1u, 0u, nz);
+        eq_table(ws.eqc, rz1, nullptr, 1u, 0u, nz);
         const uint64_t OL = C.out_rows(L - 1);
         c.launch(K_WSUM, 4.0 * N * OL + 4.0 * R * OL, [&] {
-            return launch_wsum(R, vals[L], OL, c.eqc.as<uint32_t>(), g, c.block, c.cta_budget(), c.red(),
-                               c.cv.as<uint32_t>(), c.stream);
+            return launch_wsum(R, vals[L], OL, ws.eqc, gk[K_WSUM], X.block, ck_ctas[K_WSUM], red(), ws.cv, c.stream);
         });
-        c.copy(c.h_cv.p, c.cv.p, R * rowb, cudaMemcpyDeviceToHost, "claims readback");
+        c.copy(c.h_cv.p, ws.cv, R * rowb, cudaMemcpyDeviceToHost, "claims readback");
         c.sync();
         require_canonical();
         memcpy(claimed_v, c.h_cv.p, R * rowb);
@@ -753,7 +856,7 @@ struct Prover {
 
     void evaluate_only(const uint32_t* h_input, uint32_t* out, bool all_layers) {
         const uint64_t rowb = (uint64_t)N * 4;
-        reserve(true);
+        reserve(true, false);
         layout_values(nullptr);
         c.copy(vals[0], h_input, C.in_rows(0) * rowb, cudaMemcpyHostToDevice, "input upload");
         check_input();
@@ -762,10 +865,11 @@ struct Prover {
         require_canonical();
         const size_t L = C.layers.size();
         if (all_layers) {
-            ck(cudaMemcpy(out, vals[0], C.value_rows() * rowb, cudaMemcpyDeviceToHost), "values readback");
+            c.copy(out, vals[0], C.value_rows() * rowb, cudaMemcpyDeviceToHost, "values readback");
         } else {
-            ck(cudaMemcpy(out, vals[L], C.out_rows(L - 1) * rowb, cudaMemcpyDeviceToHost), "output readback");
+            c.copy(out, vals[L], C.out_rows(L - 1) * rowb, cudaMemcpyDeviceToHost, "output readback");
         }
+        c.sync();
         c.resolve_events();
     }
 };
@@ -781,8 +885,11 @@ void check_run(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies
     if (n_copies < 4 || n_copies % 4 || n_copies > (1u << 16))
         fail(GKRGPU_ERR_INVALID, "n_copies must be a multiple of 4 in [4, 65536], got %u", n_copies);
     const uint32_t Q = n_copies / 4;
-    const Geo g = ctx->geo(n_copies);
-    if (g.tpr * (Q / g.tpr) != Q) fail(GKRGPU_ERR_INVALID, "no row tile divides %u copies", n_copies);
+    for (int k = 0; k < K_NUM_KERNELS; k++) {
+        const Geo g = ctx->geo(n_copies, k);
+        if (g.tpr * (Q / g.tpr) != Q) fail(GKRGPU_ERR_INVALID, "no row tile divides %u copies", n_copies);
+        if (Q / g.tpr > 1024) fail(GKRGPU_ERR_INVALID, "more than 1024 lane groups; raise threads_per_row");
+    }
 }
 
 uint64_t proof_bytes(const gkrgpu_circuit* c, uint32_t N, int R) {
@@ -793,10 +900,9 @@ uint64_t proof_bytes(const gkrgpu_circuit* c, uint32_t N, int R) {
 
 // ------------------------------------------------------------------ job pipeline
 // A proof is two stages: the host stage (RAW commitment bytes into the proof buffer, their
-// SHA-256, grinding) and the device stage (upload, evaluate, then gkr_prove resuming the
-// transcript).  The device stage of proof k runs on the GPU worker while host workers
-// hash the commitments of proofs k+1, k+2, ...; device stages run one at a time in
-// submission order because they share the context's workspace.
+// SHA-256, grinding) and the device stage (workspace, upload, evaluate, then gkr_prove
+// resuming the transcript).  Host workers run host stages in submission order; each lane
+// worker takes the next queued device stage once the proof's workspace fits the budget.
 
 // Copies n bytes in helper threads while this thread hashes the source.
 void parallel_copy_and_hash(uint8_t* dst, const uint8_t* src, uint64_t n, uint8_t digest[32]) {
@@ -868,7 +974,7 @@ void host_worker(gkrgpu_ctx* c) {
     if (s) cudaStreamDestroy(s);
 }
 
-void gpu_worker(gkrgpu_ctx* c) {
+void gpu_worker(gkrgpu_ctx* c, Lane* lane) {
     cudaSetDevice(c->device);
     for (;;) {
         gkrgpu_job* j;
@@ -878,12 +984,14 @@ void gpu_worker(gkrgpu_ctx* c) {
             if (c->gpu_q.empty()) break;
             j = c->gpu_q.front();
             c->gpu_q.pop_front();
-            c->gpu_busy = true;
+            c->running++;
         }
         int rc = GKRGPU_OK;
         std::string err;
+        const uint64_t need = workspace_bytes(*j->circuit, j->N, j->R, j->d_input == nullptr, true);
+        c->acquire_hbm(need);
         try {
-            Prover p(*c, *j->circuit, j->N, j->R);
+            Prover p(*c, *lane, *j->circuit, j->N, j->R);
             p.device_front(j->h_input, j->d_input);
             {
                 std::unique_lock<std::mutex> lk(j->m);
@@ -892,8 +1000,9 @@ void gpu_worker(gkrgpu_ctx* c) {
             if (j->host_rc) throw Error(j->host_rc, j->host_err);
             p.device_back(j->ts, j->proof_out, j->claimed_v);
             if (j->marker >= 0) {
+                std::lock_guard<std::mutex> lk(c->stats_m);
                 if (!c->markers[j->marker]) ck(cudaEventCreate(&c->markers[j->marker]), "cudaEventCreate");
-                ck(cudaEventRecord(c->markers[j->marker], c->stream), "cudaEventRecord");
+                ck(cudaEventRecord(c->markers[j->marker], lane->stream), "cudaEventRecord");
             }
         } catch (const Error& e) {
             rc = e.code;
@@ -902,10 +1011,11 @@ void gpu_worker(gkrgpu_ctx* c) {
             rc = GKRGPU_ERR_STATE;
             err = e.what();
         }
-        if (rc != GKRGPU_OK) {
-            cudaStreamSynchronize(c->stream);
-            c->discard_job_stats();
-        }
+        // The workspace was returned to the pool (stream-ordered) when the Prover went out of
+        // scope; once the stream has passed that point the budget is released.
+        cudaStreamSynchronize(lane->stream);
+        if (rc != GKRGPU_OK) lane->discard_job_stats();
+        c->release_hbm(need);
         {
             std::lock_guard<std::mutex> lk(j->m);
             j->rc = rc;
@@ -915,7 +1025,7 @@ void gpu_worker(gkrgpu_ctx* c) {
         j->cv.notify_all();
         {
             std::lock_guard<std::mutex> lk(c->qm);
-            c->gpu_busy = false;
+            c->running--;
         }
         c->qcv.notify_all();
     }
@@ -982,13 +1092,22 @@ int prove_entry(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copie
     return wait_job(j, proof_len);
 }
 
+// Runs f on lane 0 with every queued proof finished first (the synchronous entry points).
+template <class F>
+void on_idle_lane(gkrgpu_ctx* ctx, F&& f) {
+    ctx->drain();
+    std::lock_guard<std::mutex> lk(ctx->qm);  // keeps workers from starting while lane 0 is used
+    DeviceGuard dg(ctx->device);
+    f(ctx->lane(0));
+}
+
 }  // namespace
 
 void gkrgpu_ctx::start_workers() {
     std::lock_guard<std::mutex> lk(qm);
     if (!workers.empty()) return;
     stopping = false;
-    workers.emplace_back(gpu_worker, this);
+    for (int i = 0; i < n_lanes; i++) workers.emplace_back(gpu_worker, this, &lane(i));
     for (int i = 0; i < host_workers; i++) workers.emplace_back(host_worker, this);
 }
 
@@ -1003,7 +1122,7 @@ extern "C" {
 const char* gkrgpu_last_error(void) { return g_last_error.c_str(); }
 
 const char* gkrgpu_version(void) {
-    static std::string v = std::string("gkrgpu 0.1 (sm_103a; host sha256: ") + sha256_impl_name() + ")";
+    static std::string v = std::string("gkrgpu 0.2 (sm_103a; host sha256: ") + sha256_impl_name() + ")";
     return v.c_str();
 }
 
@@ -1017,16 +1136,23 @@ int gkrgpu_create(int device, gkrgpu_ctx** out) {
         ck(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
         if (device < 0 || device >= n) fail(GKRGPU_ERR_INVALID, "device %d out of range (%d devices)", device, n);
         DeviceGuard dg(device);
-        gkrgpu_ctx* c = new gkrgpu_ctx();
+        std::unique_ptr<gkrgpu_ctx> c(new gkrgpu_ctx());
         c->device = device;
         cudaDeviceProp prop;
         if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) c->sm_count = prop.multiProcessorCount;
-        cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-        if (e != cudaSuccess) {
-            delete c;
-            ck(e, "cudaStreamCreate");
-        }
-        *out = c;
+        size_t free_b = 0, total_b = 0;
+        ck(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+        c->hbm_budget = (uint64_t)(free_b * 0.9);
+        cudaMemPoolProps pp;
+        memset(&pp, 0, sizeof(pp));
+        pp.allocType = cudaMemAllocationTypePinned;
+        pp.location.type = cudaMemLocationTypeDevice;
+        pp.location.id = device;
+        ck(cudaMemPoolCreate(&c->pool, &pp), "cudaMemPoolCreate");
+        uint64_t keep = c->hbm_budget;
+        ck(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
+        c->lane(0);
+        *out = c.release();
     });
 }
 
@@ -1034,9 +1160,48 @@ void gkrgpu_destroy(gkrgpu_ctx* ctx) {
     if (!ctx) return;
     try {
         ctx->shutdown();
+        DeviceGuard dg(ctx->device);
         delete ctx;
     } catch (...) {
     }
+}
+
+int gkrgpu_set_concurrency(gkrgpu_ctx* ctx, int lanes, uint64_t hbm_budget_bytes) {
+    return guarded([&] {
+        check_ctx(ctx);
+        if (lanes < 0 || lanes > 64) fail(GKRGPU_ERR_INVALID, "lanes must be in [1, 64] (0 keeps the current value)");
+        ctx->drain();
+        ctx->shutdown();
+        DeviceGuard dg(ctx->device);
+        if (lanes) {
+            ctx->n_lanes = lanes;
+            ctx->host_workers = std::max(2, std::min(lanes, 8));
+        }
+        if (hbm_budget_bytes) {
+            ctx->hbm_budget = hbm_budget_bytes;
+            uint64_t keep = hbm_budget_bytes;
+            ck(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
+        }
+        {
+            std::lock_guard<std::mutex> lk(ctx->qm);
+            ctx->stopping = false;
+        }
+    });
+}
+
+int gkrgpu_memory_stats(gkrgpu_ctx* ctx, uint64_t* in_use, uint64_t* peak, uint64_t* budget) {
+    return guarded([&] {
+        check_ctx(ctx);
+        std::lock_guard<std::mutex> lk(ctx->mem_m);
+        if (in_use) *in_use = ctx->hbm_in_use;
+        if (peak) *peak = ctx->hbm_peak;
+        if (budget) *budget = ctx->hbm_budget;
+    });
+}
+
+uint64_t gkrgpu_workspace_bytes(const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits, int input_on_device) {
+    if (!circuit) return 0;
+    return workspace_bytes(*circuit, n_copies, reps_for(grinding_bits), input_on_device == 0, true);
 }
 
 int gkrgpu_circuit_load(gkrgpu_ctx* ctx, const gkrgpu_layer_desc* layers, int n_layers, gkrgpu_circuit** out) {
@@ -1087,10 +1252,10 @@ int gkrgpu_evaluate(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_c
     return guarded([&] {
         check_run(ctx, circuit, n_copies);
         if (!input || !out) fail(GKRGPU_ERR_INVALID, "null buffer");
-        ctx->drain();
-        DeviceGuard dg(ctx->device);
-        Prover p(*ctx, *circuit, n_copies, 1);
-        p.evaluate_only(input, out, all_layers != 0);
+        on_idle_lane(ctx, [&](Lane& lane) {
+            Prover p(*ctx, lane, *circuit, n_copies, 1);
+            p.evaluate_only(input, out, all_layers != 0);
+        });
     });
 }
 
@@ -1135,7 +1300,6 @@ int gkrgpu_eval_multilinear(gkrgpu_ctx* ctx, const uint32_t* d_evals, uint32_t n
                             const uint32_t* r, int n_points, uint32_t* out) {
     return guarded([&] {
         check_ctx(ctx);
-        ctx->drain();
         if (!d_evals || !r || !out) fail(GKRGPU_ERR_INVALID, "null buffer");
         if ((uintptr_t)d_evals & 15) fail(GKRGPU_ERR_INVALID, "d_evals must be 16-byte aligned");
         if (n_points < 1 || n_points > 3) fail(GKRGPU_ERR_INVALID, "n_points must be in [1, 3]");
@@ -1145,36 +1309,43 @@ int gkrgpu_eval_multilinear(gkrgpu_ctx* ctx, const uint32_t* d_evals, uint32_t n
         for (int j = 0; j < n_points; j++)
             for (uint32_t t = 0; t < nb_vars; t++)
                 if (r[(size_t)j * nb_vars + t] >= m31::P) fail(GKRGPU_ERR_INVALID, "point coordinate >= p");
-        const Geo g = ctx->geo(n_copies);
+        const Geo g = ctx->geo(n_copies, K_WSUM);
         if (g.tpr * ((n_copies / 4) / g.tpr) != n_copies / 4) fail(GKRGPU_ERR_INVALID, "no row tile divides n_copies");
-        DeviceGuard dg(ctx->device);
-        const uint64_t rows = 1ull << nb_vars, rowb = (uint64_t)n_copies * 4;
-        ctx->eqc.ensure(n_points * rows * 4, "eq table");
-        if (ctx->acc.cap < 9ull * n_copies * 8) {
-            ctx->acc.ensure(9ull * n_copies * 8, "reduction scratch");
-            ck(cudaMemsetAsync(ctx->acc.p, 0, ctx->acc.cap, ctx->stream), "cudaMemsetAsync");
-        }
-        if (!ctx->ticket.p) {
-            ctx->ticket.ensure(256, "ticket");
-            ck(cudaMemsetAsync(ctx->ticket.p, 0, ctx->ticket.cap, ctx->stream), "cudaMemsetAsync");
-        }
-        ctx->cv.ensure(3 * rowb, "claims");
-        ctx->h_cv.ensure(3 * rowb, "pinned claims");
-        EqArgs a;
-        memset(&a, 0, sizeof(a));
-        for (int j = 0; j < n_points; j++) memcpy(a.r1[j], r + (size_t)j * nb_vars, 4 * nb_vars);
-        a.f1 = 1u;
-        a.nvars = nb_vars;
-        a.reps = n_points;
-        ctx->launch(K_EQ, 4.0 * n_points * rows, [&] { return launch_eq(ctx->eqc.as<uint32_t>(), a, ctx->stream); });
-        ctx->launch(K_WSUM, 4.0 * n_copies * rows + 4.0 * n_points * rows, [&] {
-            return launch_wsum(n_points, d_evals, rows, ctx->eqc.as<uint32_t>(), g, ctx->block, ctx->cta_budget(),
-                               ctx->red(), ctx->cv.as<uint32_t>(), ctx->stream);
+        if ((n_copies / 4) / g.tpr > 1024) fail(GKRGPU_ERR_INVALID, "more than 1024 lane groups");
+        on_idle_lane(ctx, [&](Lane& c) {
+            const uint64_t rows = 1ull << nb_vars, rowb = (uint64_t)n_copies * 4;
+            const size_t eq_b = align_up(n_points * rows * 4, 256), acc_b = align_up(9ull * n_copies * 8, 256);
+            const size_t cv_b = align_up(3 * rowb, 256), total = eq_b + acc_b + 4096 + cv_b;
+            void* p = nullptr;
+            ck(cudaMallocFromPoolAsync(&p, total, ctx->pool, c.stream), "workspace allocation");
+            char* base = static_cast<char*>(p);
+            uint32_t* eq = reinterpret_cast<uint32_t*>(base);
+            RedScratch red{reinterpret_cast<unsigned long long*>(base + eq_b),
+                           reinterpret_cast<unsigned int*>(base + eq_b + acc_b)};
+            uint32_t* cv = reinterpret_cast<uint32_t*>(base + eq_b + acc_b + 4096);
+            struct Free {
+                void* p;
+                cudaStream_t s;
+                ~Free() { cudaFreeAsync(p, s); }
+            } guard{p, c.stream};
+            ck(cudaMemsetAsync(base + eq_b, 0, acc_b + 4096, c.stream), "cudaMemsetAsync");
+            c.h_cv.ensure(3 * rowb, "pinned claims");
+            EqArgs a;
+            memset(&a, 0, sizeof(a));
+            for (int j = 0; j < n_points; j++) memcpy(a.r1[j], r + (size_t)j * nb_vars, 4 * nb_vars);
+            a.f1 = 1u;
+            a.nvars = nb_vars;
+            a.reps = n_points;
+            c.launch(K_EQ, 4.0 * n_points * rows, [&] { return launch_eq(eq, a, c.stream); });
+            c.launch(K_WSUM, 4.0 * n_copies * rows + 4.0 * n_points * rows, [&] {
+                return launch_wsum(n_points, d_evals, rows, eq, g, ctx->block, ctx->cta_budget(K_WSUM), red, cv,
+                                   c.stream);
+            });
+            c.copy(c.h_cv.p, cv, n_points * rowb, cudaMemcpyDeviceToHost, "result readback");
+            c.sync();
+            memcpy(out, c.h_cv.p, n_points * rowb);
+            c.resolve_events();
         });
-        ctx->copy(ctx->h_cv.p, ctx->cv.p, n_points * rowb, cudaMemcpyDeviceToHost, "result readback");
-        ctx->sync();
-        memcpy(out, ctx->h_cv.p, n_points * rowb);
-        ctx->resolve_events();
     });
 }
 
@@ -1209,20 +1380,20 @@ int gkrgpu_host_free(void* p) {
 int gkrgpu_memcpy_h2d(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t bytes) {
     return guarded([&] {
         check_ctx(ctx);
-        ctx->drain();
-        DeviceGuard dg(ctx->device);
-        ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
-        ctx->sync();
+        on_idle_lane(ctx, [&](Lane& c) {
+            c.copy(dst, src, bytes, cudaMemcpyHostToDevice, "cudaMemcpyAsync");
+            c.sync();
+        });
     });
 }
 
 int gkrgpu_memcpy_d2h(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t bytes) {
     return guarded([&] {
         check_ctx(ctx);
-        ctx->drain();
-        DeviceGuard dg(ctx->device);
-        ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
-        ctx->sync();
+        on_idle_lane(ctx, [&](Lane& c) {
+            c.copy(dst, src, bytes, cudaMemcpyDeviceToHost, "cudaMemcpyAsync");
+            c.sync();
+        });
     });
 }
 
@@ -1238,7 +1409,7 @@ int gkrgpu_reset_stats(gkrgpu_ctx* ctx) {
     return guarded([&] {
         check_ctx(ctx);
         ctx->drain();
-        ctx->discard_job_stats();
+        for (auto& l : ctx->lanes) l->discard_job_stats();
         std::lock_guard<std::mutex> lk(ctx->stats_m);
         for (int k = 0; k < K_NUM_KERNELS; k++) {
             ctx->launches[k] = 0;
@@ -1253,22 +1424,30 @@ int gkrgpu_mark(gkrgpu_ctx* ctx, int slot) {
     return guarded([&] {
         check_ctx(ctx);
         if (slot < 0 || slot >= 64) fail(GKRGPU_ERR_INVALID, "marker slot must be in [0, 64)");
-        DeviceGuard dg(ctx->device);
-        if (!ctx->markers[slot]) ck(cudaEventCreate(&ctx->markers[slot]), "cudaEventCreate");
-        ck(cudaEventRecord(ctx->markers[slot], ctx->stream), "cudaEventRecord");
+        on_idle_lane(ctx, [&](Lane& c) {
+            std::lock_guard<std::mutex> lk(ctx->stats_m);
+            if (!ctx->markers[slot]) ck(cudaEventCreate(&ctx->markers[slot]), "cudaEventCreate");
+            ck(cudaEventRecord(ctx->markers[slot], c.stream), "cudaEventRecord");
+        });
     });
 }
 
 int gkrgpu_elapsed_ms(gkrgpu_ctx* ctx, int from_slot, int to_slot, double* ms) {
     return guarded([&] {
         check_ctx(ctx);
-        if (!ms || from_slot < 0 || from_slot >= 64 || to_slot < 0 || to_slot >= 64 || !ctx->markers[from_slot] ||
-            !ctx->markers[to_slot])
-            fail(GKRGPU_ERR_INVALID, "unrecorded marker slot");
+        cudaEvent_t a, b;
+        {
+            std::lock_guard<std::mutex> lk(ctx->stats_m);
+            if (!ms || from_slot < 0 || from_slot >= 64 || to_slot < 0 || to_slot >= 64 || !ctx->markers[from_slot] ||
+                !ctx->markers[to_slot])
+                fail(GKRGPU_ERR_INVALID, "unrecorded marker slot");
+            a = ctx->markers[from_slot];
+            b = ctx->markers[to_slot];
+        }
         DeviceGuard dg(ctx->device);
-        ck(cudaEventSynchronize(ctx->markers[to_slot]), "cudaEventSynchronize");
+        ck(cudaEventSynchronize(b), "cudaEventSynchronize");
         float t = 0.f;
-        ck(cudaEventElapsedTime(&t, ctx->markers[from_slot], ctx->markers[to_slot]), "cudaEventElapsedTime");
+        ck(cudaEventElapsedTime(&t, a, b), "cudaEventElapsedTime");
         *ms = t;
     });
 }
@@ -1298,12 +1477,92 @@ int gkrgpu_set_tile(gkrgpu_ctx* ctx, uint32_t threads_per_row, uint32_t block, u
         check_ctx(ctx);
         ctx->drain();
         const uint32_t b = block ? block : ctx->block;
-        const uint32_t t = threads_per_row ? threads_per_row : ctx->tpr_max;
         if (b < 32 || b > 256 || b % 32) fail(GKRGPU_ERR_INVALID, "block must be a multiple of 32 in [32, 256]");
-        if (t < 1 || t > b) fail(GKRGPU_ERR_INVALID, "threads_per_row must be in [1, block]");
+        if (threads_per_row > b) fail(GKRGPU_ERR_INVALID, "threads_per_row must be in [1, block]");
         ctx->block = b;
-        ctx->tpr_max = t;
-        if (ctas) ctx->ctas = ctas;
+        for (auto& t : ctx->tiles) {
+            if (threads_per_row) t.tpr = threads_per_row;
+            if (ctas) t.ctas = ctas;
+        }
+    });
+}
+
+int gkrgpu_autotune(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
+                    const uint32_t* input, int input_on_device, gkrgpu_tile_choice* out, int cap) {
+    return guarded([&] {
+        check_run(ctx, circuit, n_copies);
+        if (!input) fail(GKRGPU_ERR_INVALID, "null input");
+        ctx->drain();
+        const int R = reps_for(grinding_bits);
+        if (R < 1 || R > 3) fail(GKRGPU_ERR_INVALID, "unsupported grinding_bits");
+        std::vector<uint8_t> proof(proof_bytes(circuit, n_copies, R));
+        std::vector<uint32_t> cv((size_t)R * n_copies);
+        const bool saved_timing = ctx->timing;
+        const auto saved_tiles = std::vector<gkrgpu_ctx::Tile>(std::begin(ctx->tiles), std::end(ctx->tiles));
+        ctx->timing = true;
+        auto snapshot = [&](double* ms) {
+            std::lock_guard<std::mutex> lk(ctx->stats_m);
+            for (int k = 0; k < K_NUM_KERNELS; k++) ms[k] = ctx->ms[k];
+        };
+        // One proof with the current tiles; returns the device ms of each kernel kind.
+        auto run = [&](double* ms) {
+            double a[K_NUM_KERNELS], b[K_NUM_KERNELS];
+            snapshot(a);
+            uint64_t len = 0;
+            const int rc = prove_entry(ctx, circuit, n_copies, grinding_bits, input_on_device ? nullptr : input,
+                                       input_on_device ? input : nullptr, proof.data(), proof.size(), &len, cv.data());
+            if (rc != GKRGPU_OK) throw Error(rc, g_last_error);
+            snapshot(b);
+            for (int k = 0; k < K_NUM_KERNELS; k++) ms[k] = b[k] - a[k];
+        };
+        const int kinds[] = {K_EVALUATE, K_HG_ROUND0, K_ROUND_LANE, K_ROUND_SCALAR, K_WSUM};
+        try {
+            double ms[K_NUM_KERNELS];
+            run(ms);  // warm-up: pool growth, first-launch costs
+            // stage 1: threads per row (distinct effective tiles only), default CTA budgets
+            double best_ms[K_NUM_KERNELS];
+            uint32_t best_tpr[K_NUM_KERNELS], best_ctas[K_NUM_KERNELS];
+            for (int k = 0; k < K_NUM_KERNELS; k++) {
+                best_ms[k] = 1e300;
+                best_tpr[k] = saved_tiles[k].tpr;
+                best_ctas[k] = 0;
+            }
+            std::vector<uint32_t> seen;
+            for (uint32_t t : {8u, 16u, 32u, 64u, 128u}) {
+                for (auto& tl : ctx->tiles) tl = gkrgpu_ctx::Tile{t, 0};
+                const uint32_t eff = ctx->geo(n_copies, K_ROUND_LANE).tpr;
+                if (std::find(seen.begin(), seen.end(), eff) != seen.end()) continue;
+                seen.push_back(eff);
+                run(ms);
+                for (int k : kinds)
+                    if (ms[k] > 0 && ms[k] < best_ms[k]) {
+                        best_ms[k] = ms[k];
+                        best_tpr[k] = t;
+                    }
+            }
+            // stage 2: CTA budgets with each kind's best tile
+            for (uint32_t m : {2u, 8u, 16u}) {
+                for (int k = 0; k < K_NUM_KERNELS; k++) ctx->tiles[k] = gkrgpu_ctx::Tile{best_tpr[k], m * ctx->sm_count};
+                run(ms);
+                for (int k : kinds)
+                    if (ms[k] > 0 && ms[k] < best_ms[k]) {
+                        best_ms[k] = ms[k];
+                        best_ctas[k] = m * ctx->sm_count;
+                    }
+            }
+            for (int k = 0; k < K_NUM_KERNELS; k++) ctx->tiles[k] = gkrgpu_ctx::Tile{best_tpr[k], best_ctas[k]};
+            if (out)
+                for (int k = 0; k < K_NUM_KERNELS && k < cap; k++) {
+                    out[k].threads_per_row = ctx->geo(n_copies, k).tpr;
+                    out[k].ctas = ctx->cta_budget(k);
+                    out[k].ms = best_ms[k] < 1e300 ? best_ms[k] : 0.0;
+                }
+        } catch (...) {
+            for (int k = 0; k < K_NUM_KERNELS; k++) ctx->tiles[k] = saved_tiles[k];
+            ctx->timing = saved_timing;
+            throw;
+        }
+        ctx->timing = saved_timing;
     });
 }
 

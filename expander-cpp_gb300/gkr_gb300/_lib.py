@@ -32,6 +32,10 @@ class LayerDesc(ctypes.Structure):
                 ("mul", ctypes.c_void_p), ("add", ctypes.c_void_p)]
 
 
+class TileChoice(ctypes.Structure):
+    _fields_ = [("threads_per_row", ctypes.c_uint32), ("ctas", ctypes.c_uint32), ("ms", ctypes.c_double)]
+
+
 class KernelStat(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char_p), ("launches", ctypes.c_uint64), ("total_ms", ctypes.c_double),
                 ("algorithmic_bytes", ctypes.c_double)]
@@ -54,6 +58,9 @@ SIGNATURES = [
     ("gkrgpu_prove_device", _I, [_P, _P, _U32, _I, _P, _P, _U64, ctypes.POINTER(_U64), _P]),
     ("gkrgpu_prove_submit", _I, [_P, _P, _U32, _I, _P, _I, _P, _U64, _P, _I, ctypes.POINTER(_P)]),
     ("gkrgpu_prove_wait", _I, [_P, ctypes.POINTER(_U64)]),
+    ("gkrgpu_set_concurrency", _I, [_P, _I, _U64]),
+    ("gkrgpu_workspace_bytes", _U64, [_P, _U32, _I, _I]),
+    ("gkrgpu_memory_stats", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     ("gkrgpu_eval_multilinear", _I, [_P, _P, _U32, _U32, _P, _I, _P]),
     ("gkrgpu_eval_multilinear_noalloc", _I, [_P, _U32, _U32, _P, _I, _P, _P]),
     ("gkrgpu_device_alloc", _I, [_P, _U64, ctypes.POINTER(_P)]),
@@ -66,6 +73,7 @@ SIGNATURES = [
     ("gkrgpu_reset_stats", _I, [_P]),
     ("gkrgpu_kernel_stats", _I, [_P, _P, _I]),
     ("gkrgpu_set_tile", _I, [_P, _U32, _U32, _U32]),
+    ("gkrgpu_autotune", _I, [_P, _P, _U32, _I, _P, _I, _P, _I]),
     ("gkrgpu_mark", _I, [_P, _I]),
     ("gkrgpu_elapsed_ms", _I, [_P, _I, _I, ctypes.POINTER(ctypes.c_double)]),
     ("gkrgpu_transfer_stats", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),

@@ -204,6 +204,30 @@ class Context:
     def set_tile(self, threads_per_row=0, block=0, ctas=0):
         _lib.check(_lib.load().gkrgpu_set_tile(self.handle, threads_per_row, block, ctas))
 
+    def autotune(self, dc: DeviceCircuit, witness=None, n_copies=None, d_input=None, grinding_bits=10):
+        """gkrgpu_autotune: picks each kernel kind's row tile by timing whole proofs.  Returns
+        {kernel: {"threads_per_row", "ctas", "ms"}}."""
+        lib = _lib.load()
+        arr = (_lib.TileChoice * 32)()
+        if d_input is not None:
+            src, on_dev, n, keep = ctypes.c_void_p(d_input), 1, n_copies, None
+        else:
+            keep = np.ascontiguousarray(witness, dtype=np.uint32)
+            src, on_dev, n = keep.ctypes.data, 0, keep.shape[1]
+        _lib.check(lib.gkrgpu_autotune(self.handle, dc.handle, n, grinding_bits, src, on_dev, arr, 32))
+        names = list(self.kernel_stats().keys())
+        return {names[i]: {"threads_per_row": arr[i].threads_per_row, "ctas": arr[i].ctas, "ms": arr[i].ms}
+                for i in range(len(names))}
+
+    def set_concurrency(self, lanes=0, hbm_budget_bytes=0):
+        """Device stages of up to `lanes` proofs run at once under an HBM budget."""
+        _lib.check(_lib.load().gkrgpu_set_concurrency(self.handle, lanes, hbm_budget_bytes))
+
+    def memory_stats(self):
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _lib.check(_lib.load().gkrgpu_memory_stats(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"in_use": a.value, "peak": b.value, "budget": c.value}
+
     def mark(self, slot: int):
         """Records timing marker `slot` on the context's stream."""
         _lib.check(_lib.load().gkrgpu_mark(self.handle, slot))

@@ -116,6 +116,21 @@ int gkrgpu_prove_device(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
  * gkrgpu_prove_device are submit + wait.  No counterpart in the reference (one proof per
  * thread there, bench_keccak.cpp:82-93). */
 typedef struct gkrgpu_job gkrgpu_job;
+
+/* Continuous batching.  A context runs the device stages of up to `lanes` proofs at once,
+ * each on its own stream (default 1); a queued proof starts when a lane is free and its
+ * device workspace (gkrgpu_workspace_bytes) fits in `hbm_budget_bytes` next to the proofs
+ * already running (a proof larger than the budget runs alone).  Workspaces come from a
+ * stream-ordered pool and are returned when the proof ends.  Waits for queued proofs
+ * first; 0 keeps the current value (default budget: 90% of the free memory at creation).
+ * No counterpart in the reference, which proves one circuit per thread. */
+int gkrgpu_set_concurrency(gkrgpu_ctx* ctx, int lanes, uint64_t hbm_budget_bytes);
+/* Device bytes one proof of this circuit holds while it runs. */
+uint64_t gkrgpu_workspace_bytes(const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
+                                int input_on_device);
+/* Workspace bytes held now, the peak since creation, and the budget. */
+int gkrgpu_memory_stats(gkrgpu_ctx* ctx, uint64_t* in_use, uint64_t* peak, uint64_t* budget);
+
 int gkrgpu_prove_submit(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
                         const uint32_t* input, int input_on_device, uint8_t* proof_out, uint64_t proof_cap,
                         uint32_t* claimed_v, int marker_slot, gkrgpu_job** job);
@@ -169,6 +184,19 @@ int gkrgpu_kernel_stats(gkrgpu_ctx* ctx, gkrgpu_kernel_stat* out, int cap);
 /* Tuning of the row tile: threads per row slice (each covers 4 copies), CTA size and the
  * CTA budget of the reducing kernels.  0 keeps the current value. */
 int gkrgpu_set_tile(gkrgpu_ctx* ctx, uint32_t threads_per_row, uint32_t block, uint32_t ctas);
+
+/* Autotuner.  Times whole proofs of `circuit` on `input` (host memory, or device memory with
+ * input_on_device = 1) with candidate row tiles - threads per row slice 8..128 (copies per
+ * CTA row tile = 4x that), then CTA budgets 2..16 x the SM count - and keeps, for each kernel
+ * kind, the tile with the least device time; tiles never change the proof bytes.  out
+ * (optional, up to cap entries, one per kernel kind in gkrgpu_kernel_stats order) receives
+ * the chosen tiles and their device ms per proof.  About 9 proofs of work. */
+typedef struct {
+    uint32_t threads_per_row, ctas;
+    double ms;
+} gkrgpu_tile_choice;
+int gkrgpu_autotune(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
+                    const uint32_t* input, int input_on_device, gkrgpu_tile_choice* out, int cap);
 
 /* Timing markers: gkrgpu_mark records CUDA event `slot` (0..63) on the context's stream;
  * gkrgpu_elapsed_ms waits for `to_slot` and returns the device time between the two. */
