@@ -55,7 +55,17 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--depth", type=int, default=3, help="proofs in flight (host hashing overlaps device work)")
-    ap.add_argument("--tile", default="", help="threads_per_row,block,ctas for every kernel (default: library's)")
+    ap.add_argument("--tile", default="", help="threads_per_row,block,ctas for every kernel (default: autotuned)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the library's default row tiles")
+    ap.add_argument("--workload", choices=["plain", "mixed", "serve"], default="plain",
+                    help="plain: the large single-circuit proof; mixed: many independent proofs of mixed depth, "
+                         "width and copies, plain one-at-a-time vs continuous batching; serve: open-loop Poisson "
+                         "arrivals of mixed proofs")
+    ap.add_argument("--proofs", type=int, default=512, help="mixed/serve: number of distinct proofs")
+    ap.add_argument("--lanes", type=int, default=16, help="mixed/serve: proofs whose device stages overlap")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="mixed/serve: device-memory admission budget")
+    ap.add_argument("--rates", default="200,500,1000,2000", help="serve: arrival rates (requests/s)")
+    ap.add_argument("--duration", type=float, default=4.0, help="serve: seconds of arrivals per rate")
     return ap.parse_args()
 
 
@@ -289,6 +299,16 @@ def run_ours(args, D):
     pbufs = [HostBuffer(plen) for _ in range(depth)]
     bufs = [(pb.array, np.empty((3, N), np.uint32)) for pb in pbufs]
 
+    # row tiles from the autotuner (whole proofs timed per candidate; outside the timed region)
+    tiles = None
+    if not args.tile and not args.no_autotune:
+        t0 = time.perf_counter()
+        tiles = ctx.autotune(dc, None, n_copies=N, d_input=din.ptr)
+        tiles = {"seconds": time.perf_counter() - t0,
+                 "choice": {k: {"threads_per_row": v["threads_per_row"], "ctas": v["ctas"]}
+                            for k, v in tiles.items() if v["ms"] > 0}}
+        ctx.reset_stats()
+
     # ---- value: input resident in HBM
     ctx.set_timing(True)
     clocks = ClockSampler(device)
@@ -359,7 +379,7 @@ def run_ours(args, D):
                 "config": dict(cfg, parallelism=f"replicas x{D.world}" if D.world > 1 else "single",
                                pipeline=f"{depth} proofs in flight; timed region = device end of the last warm-up "
                                         "proof to device end of the last timed proof"),
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "autotune": tiles,
                 "clocks": clk,
                 "latency_ms": {"p50": statistics.median(lat_ms), "p99": float(np.percentile(lat_ms, 99)),
                                "device_ms_per_proof": step_ms},
@@ -371,12 +391,175 @@ def run_ours(args, D):
         print(json.dumps(line), flush=True)
 
 
+class MixedSet:
+    """The mixed workload: independent proofs of uniform depth 4..24, width 2^8..2^18 and
+    16..256 copies (multiples of 16), 50% mul / 50% add fan-in-2 gates with uniform wiring,
+    each with its own seed; circuits resident on the device, witnesses in host memory."""
+
+    def __init__(self, ctx, n_proofs, seed=3):
+        from concurrent.futures import ThreadPoolExecutor
+
+        from gkr_gb300 import circuit as gc
+        self.specs = gc.mixed_batch_specs(seed=seed, n_proofs=n_proofs)
+        with ThreadPoolExecutor(8) as ex:
+            self.circuits = list(ex.map(lambda s: gc.uniform_circuit(s[0], s[1], s[2]), self.specs))
+            self.witness = list(ex.map(lambda s: gc.random_witness(s[0], s[2], s[3]), self.specs))
+        self.dcs = [ctx.load(c) for c in self.circuits]
+        self.proofs = [np.empty(dc.proof_size(s[3]), np.uint8) for dc, s in zip(self.dcs, self.specs)]
+        self.claims = [np.empty((3, s[3]), np.uint32) for s in self.specs]
+        self.bytes = sum(s[1] * (1 << s[2]) * s[3] * 4 for s in self.specs)
+
+    def submit(self, ctx, i):
+        return ctx.submit(self.dcs[i], self.witness[i], self.proofs[i], self.claims[i])
+
+    def digests(self, idx):
+        import hashlib
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(8) as ex:
+            return list(ex.map(lambda i: hashlib.sha256(self.proofs[i].tobytes()).hexdigest(), idx))
+
+
+def run_mixed(args, D):
+    """Plain (one proof at a time) vs continuous batching on the same independent proofs."""
+    from gkr_gb300.prover import Context
+    if D.rank != 0:
+        return
+    ctx = Context(D.local_rank)
+    t0 = time.perf_counter()
+    ms = MixedSet(ctx, args.proofs)
+    setup_s = time.perf_counter() - t0
+    n = len(ms.specs)
+    idx = list(range(n))
+
+    # plain: one proof's device stage at a time, each proof submitted after the previous one
+    # finished (the reference's one-proof-per-call usage, on the GPU)
+    ctx.set_concurrency(lanes=1)
+    for i in range(min(4, n)):
+        ctx.wait(ms.submit(ctx, i))
+    lat_plain = []
+    t0 = time.perf_counter()
+    for i in idx:
+        t1 = time.perf_counter()
+        ctx.wait(ms.submit(ctx, i))
+        lat_plain.append((time.perf_counter() - t1) * 1000.0)
+    plain_s = time.perf_counter() - t0
+    ref = ms.digests(idx)
+
+    # batched: every proof queued at once; up to `lanes` device stages overlap, admitted by
+    # the HBM budget as earlier proofs finish
+    budget = int(args.budget_gb * (1 << 30))
+    ctx.set_concurrency(lanes=args.lanes, hbm_budget_bytes=budget)
+    warm = [ms.submit(ctx, i) for i in range(min(2 * args.lanes, n))]
+    for j in warm:
+        ctx.wait(j)
+    clocks = ClockSampler(D.local_rank)
+    clocks.start()
+    t0 = time.perf_counter()
+    sub = {}
+    jobs = []
+    for i in idx:
+        sub[i] = time.perf_counter()
+        jobs.append(ms.submit(ctx, i))
+    done = []
+    for i, j in zip(idx, jobs):
+        ctx.wait(j)
+        done.append((time.perf_counter() - sub[i]) * 1000.0)
+    batch_s = time.perf_counter() - t0
+    clk = clocks.stop()
+    same = ms.digests(idx) == ref
+    mem = ctx.memory_stats()
+    value = n / batch_s
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": n, "warmup": len(warm),
+            "ms_per_step": batch_s * 1000.0 / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u32", "data": "synthetic",
+            "config": {"workload": f"{n} independent proofs, depth 4..24, width 2^8..2^18, 16..256 copies, "
+                                   "50% mul uniform wiring, own seed each (one batch)",
+                       "lanes": args.lanes, "hbm_budget_bytes": budget, "setup_s": setup_s,
+                       "witness_bytes_total": ms.bytes,
+                       "timing": "host wall clock from the first submit to the last proof returned"},
+            "batched": {"proofs_per_s": value, "seconds": batch_s,
+                        "latency_ms": {"p50": statistics.median(done), "p99": float(np.percentile(done, 99))}},
+            "plain": {"proofs_per_s": n / plain_s, "seconds": plain_s,
+                      "latency_ms": {"p50": statistics.median(lat_plain), "p99": float(np.percentile(lat_plain, 99))}},
+            "batched_over_plain": (n / batch_s) / (n / plain_s), "byte_identical_to_plain": same,
+            "hbm": {"workspace_peak_bytes": mem["peak"], "budget": mem["budget"]}, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args, D):
+    """Open-loop Poisson arrivals of mixed proofs: continuous batching vs one at a time."""
+    import threading as th
+
+    from gkr_gb300.prover import Context
+    if D.rank != 0:
+        return
+    ctx = Context(D.local_rank)
+    ms = MixedSet(ctx, args.proofs, seed=5)
+    n = len(ms.specs)
+    budget = int(args.budget_gb * (1 << 30))
+    out = {}
+    for mode, lanes in (("batched", args.lanes), ("plain", 1)):
+        ctx.set_concurrency(lanes=lanes, hbm_budget_bytes=budget)
+        for i in range(min(lanes, n)):
+            ctx.wait(ms.submit(ctx, i))
+        res = {}
+        for rate in [float(r) for r in args.rates.split(",")]:
+            rng = np.random.default_rng(int(rate))
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * args.duration) + 1))
+            arrivals = arrivals[arrivals < args.duration][: 2 * n]  # bounded so the slow mode drains
+            # each request proves proof (k mod n); a proof's buffers are reused only after its
+            # previous request finished
+            busy = [th.Lock() for _ in range(n)]
+            lats, lock = [], th.Lock()
+            pending = []
+
+            def waiter(job, t_arr, k):
+                ctx.wait(job)
+                t = time.perf_counter()
+                busy[k].release()
+                with lock:
+                    lats.append((t - t_arr) * 1000.0)
+
+            t0 = time.perf_counter()
+            for r, a in enumerate(arrivals):
+                now = time.perf_counter() - t0
+                if a > now:
+                    time.sleep(a - now)
+                k = r % n
+                busy[k].acquire()
+                t_arr = t0 + a
+                job = ms.submit(ctx, k)
+                w = th.Thread(target=waiter, args=(job, t_arr, k))
+                w.start()
+                pending.append(w)
+            for w in pending:
+                w.join()
+            wall = time.perf_counter() - t0
+            res[str(int(rate))] = {"offered": len(arrivals), "offered_per_s": len(arrivals) / args.duration,
+                                   "completed_per_s": len(lats) / wall,
+                                   "latency_ms": {"p50": statistics.median(lats), "p99": float(np.percentile(lats, 99))}}
+        out[mode] = res
+    top = out["batched"][str(int(float(args.rates.split(",")[-1])))]
+    line = {"metric": METRIC, "value": top["completed_per_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": top["offered"], "warmup": args.lanes, "ms_per_step": 1000.0 / top["completed_per_s"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": f"open-loop Poisson arrivals over {n} distinct mixed proofs (depth 4..24, width "
+                                   "2^8..2^18, 16..256 copies)", "rates": args.rates, "duration_s": args.duration,
+                       "lanes": args.lanes, "hbm_budget_bytes": budget},
+            "serving": out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     D = Dist()
     try:
         if args.impl == "reference":
             run_reference(args, D)
+        elif args.workload == "mixed":
+            run_mixed(args, D)
+        elif args.workload == "serve":
+            run_serve(args, D)
         else:
             run_ours(args, D)
     finally:

@@ -243,7 +243,7 @@ __device__ __forceinline__ void accum_pair(uint32_t (&acc)[3][4], const uint32_t
 // v[y] * w_j[k], written for the later folds, then the round-0 sums of v(x) hg_j(x).
 // All repetitions in one thread: each gathered v[y] row serves the R weights.
 template <int R>
-__global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict__ v, uint64_t I,
+__global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ v, uint64_t I,
                                                       const uint32_t* __restrict__ mx_off, const uint4* __restrict__ mx_g,
                                                       const uint4* __restrict__ a4, const uint4* __restrict__ w4,
                                                       uint32_t* hg0, uint32_t* hg1, uint32_t* hg2, Geo g,
@@ -361,6 +361,75 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, con
         }
     }
     reduce_group<3>(acc, g, t.active, red, 3 * j, RoundFin{red, evals_out, LANE_HG ? nullptr : vx, g.N, reps});
+}
+
+// Shared-source rounds (phase-1 round 1, phase-2 rounds 0 and 1) with every repetition in
+// one thread: the layer input rows are read once for all R repetitions instead of once per
+// repetition-CTA.  Same semantics as k_round<true, LANE_HG, FOLD>.
+template <int R, bool LANE_HG, bool FOLD>
+__global__ void __launch_bounds__(256) k_round_shared(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx,
+                                                      Geo g, RedScratch red, uint32_t* evals_out) {
+    const TileIdx t = tile_idx(g);
+    const uint32_t* __restrict__ fs = p.fsrc[0];
+    uint32_t acc[3 * R][4] = {};
+    if (t.active) {
+        for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
+            uint4 a[4];
+            if (FOLD) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) a[k] = ld4(fs, 4 * i + k, g.N, t.lane0);
+            } else {
+                a[0] = ld4(fs, 2 * i, g.N, t.lane0);
+                a[1] = ld4(fs, 2 * i + 1, g.N, t.lane0);
+            }
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                const uint32_t r = p.r[j];
+                uint32_t f0[4], f1[4], h0[4], h1[4];
+                if (FOLD) {
+#pragma unroll
+                    for (int l = 0; l < 4; l++) {
+                        f0[l] = fold(comp(a[0], l), comp(a[1], l), r);
+                        f1[l] = fold(comp(a[2], l), comp(a[3], l), r);
+                    }
+                    st4(p.fdst[j], 2 * i, g.N, t.lane0, mk4(f0));
+                    st4(p.fdst[j], 2 * i + 1, g.N, t.lane0, mk4(f1));
+                } else {
+#pragma unroll
+                    for (int l = 0; l < 4; l++) { f0[l] = comp(a[0], l); f1[l] = comp(a[1], l); }
+                }
+                if (LANE_HG) {
+                    uint4 b[4];
+#pragma unroll
+                    for (int k = 0; k < 4; k++) b[k] = ld4(p.hsrc[j], 4 * i + k, g.N, t.lane0);
+#pragma unroll
+                    for (int l = 0; l < 4; l++) {
+                        h0[l] = fold(comp(b[0], l), comp(b[1], l), r);
+                        h1[l] = fold(comp(b[2], l), comp(b[3], l), r);
+                    }
+                    st4(p.hdst[j], 2 * i, g.N, t.lane0, mk4(h0));
+                    st4(p.hdst[j], 2 * i + 1, g.N, t.lane0, mk4(h1));
+                } else if (FOLD) {
+                    const uint4 s = __ldg(reinterpret_cast<const uint4*>(p.hsrc[j]) + i);
+                    const uint32_t s0 = fold(s.x, s.y, r), s1 = fold(s.z, s.w, r);
+                    if (t.q == 0 && blockIdx.y == 0) *reinterpret_cast<uint2*>(p.hdst[j] + 2 * i) = make_uint2(s0, s1);
+#pragma unroll
+                    for (int l = 0; l < 4; l++) { h0[l] = s0; h1[l] = s1; }
+                } else {
+                    const uint2 s = __ldg(reinterpret_cast<const uint2*>(p.hsrc[j]) + i);
+#pragma unroll
+                    for (int l = 0; l < 4; l++) { h0[l] = s.x; h1[l] = s.y; }
+                }
+#pragma unroll
+                for (int l = 0; l < 4; l++) {
+                    acc[3 * j][l] = add(acc[3 * j][l], mul(f0[l], h0[l]));
+                    acc[3 * j + 1][l] = add(acc[3 * j + 1][l], mul(f1[l], h1[l]));
+                    acc[3 * j + 2][l] = add(acc[3 * j + 2][l], mul(add(f0[l], f1[l]), add(h0[l], h1[l])));
+                }
+            }
+        }
+    }
+    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, LANE_HG ? nullptr : vx, g.N, (uint32_t)R});
 }
 
 // ---------------------------------------------------------------- phase two: s(y)
@@ -483,6 +552,23 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, co
     if (reps < 1 || reps > 3) return cudaErrorInvalidValue;
     if (lane_hg && !fold_) return cudaErrorInvalidValue;  // phase-one round 0 lives in k_hg_round0
     if (!fold_ && !shared_src) return cudaErrorInvalidValue;
+    if (shared_src) {
+        // one read of the shared layer input for all repetitions
+        LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
+#define GKR_SHARED(RR, LH, FO) k_round_shared<RR, LH, FO><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out)
+#define GKR_SHARED_R(RR)                                  \
+    if (lane_hg) GKR_SHARED(RR, true, true);              \
+    else if (fold_) GKR_SHARED(RR, false, true);          \
+    else GKR_SHARED(RR, false, false);
+        switch (reps) {
+            case 1: GKR_SHARED_R(1) break;
+            case 2: GKR_SHARED_R(2) break;
+            default: GKR_SHARED_R(3) break;
+        }
+#undef GKR_SHARED_R
+#undef GKR_SHARED
+        return cudaGetLastError();
+    }
     LaunchShape sh = rep_shape(g, npairs, block, ctas, reps);
 #define GKR_ROUND(SH, LH, FO) k_round<SH, LH, FO><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, reps, red, evals_out)
     if (lane_hg) {

@@ -189,6 +189,37 @@ def random_witness(seed, nb_input_vars, n_copies, out=None):
     return res
 
 
+def uniform_circuit(seed, depth, width, p_mul=0.5):
+    """`depth` layers of 2^width gates with uniform wiring, generated in one vectorised pass
+    (the mixed-batch workload builds hundreds of these)."""
+    st = Stream(seed)
+    O = I = 1 << width
+    is_mul = st.uniform(depth * O).reshape(depth, O) < p_mul
+    layers = []
+    for l in range(depth):
+        mo = np.nonzero(is_mul[l])[0].astype(np.uint64)
+        ao = np.repeat(np.nonzero(~is_mul[l])[0].astype(np.uint64), 2)
+        nm, na = len(mo), len(ao)
+        r = st.below(2 * nm + na, I)
+        c = _coefs(st, nm + na)
+        mul = np.stack([mo, r[:nm], r[nm:2 * nm], c[:nm]], axis=1).astype(np.uint32)
+        add = np.stack([ao, r[2 * nm:], c[nm:]], axis=1).astype(np.uint32)
+        layers.append(CircuitLayer(width, width, mul, add))
+    return Circuit(layers)
+
+
+def mixed_batch_specs(seed=3, n_proofs=512, depth=(4, 24), width=(8, 18), copies=(16, 256)):
+    """Per-proof (seed, depth, width, copies) of the mixed batched workload: depth and width
+    exponent uniform in their ranges, copies uniform in the range rounded down to a multiple
+    of 16."""
+    st = Stream(seed)
+    d = depth[0] + st.below(n_proofs, depth[1] - depth[0] + 1)
+    k = width[0] + st.below(n_proofs, width[1] - width[0] + 1)
+    n = copies[0] + st.below(n_proofs, copies[1] - copies[0] + 1)
+    n = np.maximum(16, (n // 16) * 16)
+    return [(int(seed * 100003 + i), int(d[i]), int(k[i]), int(n[i])) for i in range(n_proofs)]
+
+
 # ---------------------------------------------------------------- named workloads
 
 def config1_circuit(seed=1234, n_layers=8, width=10):
