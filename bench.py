@@ -535,7 +535,8 @@ def run_serve(args, D):
             for w in pending:
                 w.join()
             wall = time.perf_counter() - t0
-            res[str(int(rate))] = {"offered": len(arrivals), "offered_per_s": len(arrivals) / args.duration,
+            window = float(arrivals[-1]) if len(arrivals) > 1 else args.duration
+            res[str(int(rate))] = {"offered": len(arrivals), "offered_per_s": len(arrivals) / window,
                                    "completed_per_s": len(lats) / wall,
                                    "latency_ms": {"p50": statistics.median(lats), "p99": float(np.percentile(lats, 99))}}
         out[mode] = res
