@@ -93,6 +93,11 @@ __device__ __forceinline__ void reduce_group(const uint32_t (&acc)[C][4], const 
     const uint32_t lanes = 4 * tpr, base = blockIdx.y * lanes;
     for (uint32_t li = tid; li < lanes; li += B) fin(base + li);
     if (tid == 0) red.ticket[blockIdx.y] = 0u;
+    if (red.done) {
+        __threadfence_system();
+        __syncthreads();
+        if (tid == 0) atomicAdd_system(red.done, 1u);
+    }
 }
 
 struct TileIdx {

@@ -20,6 +20,9 @@ struct Geo {
 struct RedScratch {
     unsigned long long* acc;  // components x N
     unsigned int* ticket;
+    // Optional completion counter in host-mapped memory: each lane group's finishing CTA
+    // increments it (system scope) after its results are visible to the host.
+    unsigned int* done = nullptr;
 };
 
 struct EqArgs {

@@ -210,7 +210,57 @@ struct Lane {
     uint64_t job_launches[K_NUM_KERNELS] = {};
     double job_bytes[K_NUM_KERNELS] = {};
 
+    // Host-mapped staging for the round evaluations written by the finishing CTAs, followed
+    // by the completion counter they increment (RedScratch::done).
+    char* map_h = nullptr;
+    char* map_d = nullptr;
+    size_t map_cap = 0;
+    uint32_t done_seen = 0;
+    uint32_t* evals_h() const { return reinterpret_cast<uint32_t*>(map_h); }
+    uint32_t* evals_d() const { return reinterpret_cast<uint32_t*>(map_d); }
+    unsigned int* done_d() const { return reinterpret_cast<unsigned int*>(map_d + map_cap - 256); }
+    volatile uint32_t* done_h() const { return reinterpret_cast<volatile uint32_t*>(map_h + map_cap - 256); }
+    void ensure_mapped(size_t evals_bytes) {
+        const size_t need = align_up(evals_bytes, 256) + 256;
+        if (need <= map_cap) return;
+        if (map_h) cudaFreeHost(map_h);
+        map_h = map_d = nullptr;
+        map_cap = 0;
+        void* p = nullptr;
+        ck(cudaHostAlloc(&p, need, cudaHostAllocMapped | cudaHostAllocPortable), "mapped staging allocation");
+        map_h = static_cast<char*>(p);
+        void* d = nullptr;
+        ck(cudaHostGetDevicePointer(&d, p, 0), "cudaHostGetDevicePointer");
+        map_d = static_cast<char*>(d);
+        map_cap = need;
+        memset(map_h, 0, need);
+        done_seen = 0;
+    }
+    // The stream is idle: take the counter as consumed.
+    void resync_done() { done_seen = *done_h(); }
+    // Waits until `groups` more finishing CTAs have published their results.  A stream that
+    // went idle or failed without them is an error; the wait is bounded.
+    void wait_done(uint32_t groups) {
+        const uint32_t target = done_seen + groups;
+        const auto t0 = std::chrono::steady_clock::now();
+        for (uint64_t it = 0;; it++) {
+            if ((int32_t)(*done_h() - target) >= 0) break;
+            if ((it & 1023) == 1023) {
+                const cudaError_t e = cudaStreamQuery(stream);
+                if (e != cudaSuccess && e != cudaErrorNotReady) ck(e, "round kernel");
+                if (e == cudaSuccess && (int32_t)(*done_h() - target) < 0)
+                    fail(GKRGPU_ERR_STATE, "round kernel finished without publishing its results");
+                if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60))
+                    fail(GKRGPU_ERR_TIMEOUT, "round results not published within 60 s");
+                std::this_thread::yield();
+            }
+        }
+        std::atomic_thread_fence(std::memory_order_acquire);
+        done_seen = target;
+    }
+
     ~Lane() {
+        if (map_h) cudaFreeHost(map_h);
         for (PinnedBuf* b : {&h_evals, &h_rows, &h_vx, &h_cv, &h_flag}) b->release();
         for (auto e : events) cudaEventDestroy(e);
         if (done_ev) cudaEventDestroy(done_ev);
@@ -601,6 +651,9 @@ struct Prover {
     }
 
     RedScratch red() const { return RedScratch{ws.acc, ws.ticket}; }
+    // Round kernels publish their evaluations into the lane's mapped staging buffer.
+    RedScratch red_mapped() const { return RedScratch{ws.acc, ws.ticket, c.done_d()}; }
+    uint32_t groups(int kid) const { return N / (4 * gk[kid].tpr); }
 
     void reserve(bool own_input, bool sumcheck) {
         ws.plan(nullptr, C, N, R, own_input, sumcheck);
@@ -609,7 +662,8 @@ struct Prover {
         block = static_cast<char*>(p);
         ws.plan(block, C, N, R, own_input, sumcheck);
         ck(cudaMemsetAsync(block + ws.zero_off, 0, ws.zero_bytes, c.stream), "cudaMemsetAsync");
-        c.h_evals.ensure(9ull * N * 4, "pinned evaluations");
+        c.ensure_mapped(9ull * N * 4);
+        c.resync_done();
         c.h_rows.ensure(6ull * N * 4, "pinned rows");
         c.h_vx.ensure(3ull * N * 4, "pinned vx");
         c.h_cv.ensure(3ull * N * 4, "pinned claims");
@@ -652,17 +706,18 @@ struct Prover {
         }
     }
 
-    // D2H of the 3R evaluation rows and optionally `rows_from` rows 0..1 for each repetition.
-    void fetch(const uint32_t* const* rows_from, bool shared_rows) {
+    // Waits for the round's 3R evaluation rows (published by `groups` finishing CTAs into the
+    // mapped staging buffer) and optionally D2H-copies rows 0..1 of `rows_from` per repetition.
+    void fetch(uint32_t groups, const uint32_t* const* rows_from, bool shared_rows) {
         const uint64_t rowb = (uint64_t)N * 4;
-        c.copy(c.h_evals.p, ws.evals, 3ull * R * rowb, cudaMemcpyDeviceToHost, "fetch evals");
         if (rows_from) {
             for (int j = 0; j < R; j++) {
                 const uint32_t* src = shared_rows ? rows_from[0] : rows_from[j];
                 c.copy(c.h_rows.as<char>() + 2 * j * rowb, src, 2 * rowb, cudaMemcpyDeviceToHost, "fetch rows");
             }
         }
-        c.sync();
+        c.wait_done(groups);
+        if (rows_from) c.sync();
     }
 
     // Transcript step of one round for every repetition (sumcheck.hpp:74-96).  With
@@ -671,8 +726,17 @@ struct Prover {
     void transcript_round(Transcript& t, uint32_t (*rch)[32], uint32_t k, bool last, bool append_last,
                           uint32_t* last_out) {
         const uint64_t rowb = (uint64_t)N * 4;
+        const char* ev = reinterpret_cast<const char*>(c.evals_h());
+        if (R == 3 && !last) {
+            const uint8_t* msgs[3] = {(const uint8_t*)ev, (const uint8_t*)ev + 3 * rowb, (const uint8_t*)ev + 6 * rowb};
+            uint32_t r3[3];
+            if (t.append_challenge3(msgs, 3 * rowb, r3)) {
+                for (int j = 0; j < 3; j++) rch[j][k] = r3[j];
+                return;
+            }
+        }
         for (int j = 0; j < R; j++) {
-            t.append(c.h_evals.as<char>() + 3ull * j * rowb, 3 * rowb);
+            t.append(ev + 3ull * j * rowb, 3 * rowb);
             const uint32_t r = t.challenge();
             rch[j][k] = r;
             if (last) {
@@ -720,10 +784,10 @@ struct Prover {
         const double hb = rb * (I + Ly.nmul + (double)R * I) + 32.0 * Ly.nmul + 20.0 * I;
         c.launch(K_HG_ROUND0, hb, [&] {
             return launch_hg_round0(R, v, I, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, hg, gk[K_HG_ROUND0], X.block,
-                                    ck_ctas[K_HG_ROUND0], red(), ws.evals, c.stream);
+                                    ck_ctas[K_HG_ROUND0], red_mapped(), c.evals_d(), c.stream);
         });
         const uint32_t* vsrc[1] = {v};
-        fetch(n == 1 ? vsrc : nullptr, true);
+        fetch(groups(K_HG_ROUND0), n == 1 ? vsrc : nullptr, true);
         transcript_round(t, rx, 0, n == 1, true, vxh);
 
         const uint32_t* cur_f[3] = {v, v, v};
@@ -743,10 +807,10 @@ struct Prover {
             const double b = rb * ((k == 1 ? 1.0 : R) * S + R * S + R * S);
             c.launch(K_ROUND_LANE, b, [&] {
                 return launch_round(R, k == 1, true, true, p, npairs, nullptr, gk[K_ROUND_LANE], X.block,
-                                    ck_ctas[K_ROUND_LANE], red(), ws.evals, c.stream);
+                                    ck_ctas[K_ROUND_LANE], red_mapped(), c.evals_d(), c.stream);
             });
             const bool last = (k == n - 1);
-            fetch(last ? p.fdst : nullptr, false);
+            fetch(groups(K_ROUND_LANE), last ? p.fdst : nullptr, false);
             transcript_round(t, rx, k, last, true, vxh);
             for (int j = 0; j < R; j++) {
                 cur_f[j] = p.fdst[j];
@@ -769,9 +833,9 @@ struct Prover {
             const uint64_t npairs = I >> 1;
             c.launch(K_ROUND_SCALAR, rb * 2.0 * npairs + 8.0 * R * npairs, [&] {
                 return launch_round(R, true, false, false, p, npairs, ws.vx, gk[K_ROUND_SCALAR], X.block,
-                                    ck_ctas[K_ROUND_SCALAR], red(), ws.evals, c.stream);
+                                    ck_ctas[K_ROUND_SCALAR], red_mapped(), c.evals_d(), c.stream);
             });
-            fetch(n == 1 ? vsrc : nullptr, true);
+            fetch(groups(K_ROUND_SCALAR), n == 1 ? vsrc : nullptr, true);
             transcript_round(t, ry, 0, n == 1, false, vy.data());
         }
         for (int j = 0; j < R; j++) cur_f[j] = v;
@@ -791,10 +855,10 @@ struct Prover {
             const double b = rb * ((k == 1 ? 1.0 : R) * S + R * S / 2) + 6.0 * R * S;
             c.launch(K_ROUND_SCALAR, b, [&] {
                 return launch_round(R, k == 1, false, true, p, npairs, ws.vx, gk[K_ROUND_SCALAR], X.block,
-                                    ck_ctas[K_ROUND_SCALAR], red(), ws.evals, c.stream);
+                                    ck_ctas[K_ROUND_SCALAR], red_mapped(), c.evals_d(), c.stream);
             });
             const bool last = (k == n - 1);
-            fetch(last ? p.fdst : nullptr, false);
+            fetch(groups(K_ROUND_SCALAR), last ? p.fdst : nullptr, false);
             transcript_round(t, ry, k, last, false, vy.data());
             for (int j = 0; j < R; j++) cur_f[j] = p.fdst[j];
         }

@@ -127,6 +127,86 @@ void sha256(const uint8_t* in, size_t n, uint8_t out[32]) {
     s.final(out);
 }
 
+namespace {
+
+#if defined(GKR_SHA_ARMV8)
+void put_digest(const uint32_t h[8], uint8_t out[32]) {
+    for (int i = 0; i < 8; i++) {
+        out[4 * i] = (uint8_t)(h[i] >> 24);
+        out[4 * i + 1] = (uint8_t)(h[i] >> 16);
+        out[4 * i + 2] = (uint8_t)(h[i] >> 8);
+        out[4 * i + 3] = (uint8_t)h[i];
+    }
+}
+
+// Three independent message streams in one loop: the SHA-2 instructions of one stream
+// depend on each other, so interleaving three streams fills the pipeline.
+void compress3(uint32_t st[3][8], const uint8_t* const p[3], size_t nblocks) {
+    uint32x4_t s0[3], s1[3];
+    for (int m = 0; m < 3; m++) {
+        s0[m] = vld1q_u32(st[m]);
+        s1[m] = vld1q_u32(st[m] + 4);
+    }
+    for (size_t b = 0; b < nblocks; b++) {
+        uint32x4_t w[3][4], save0[3], save1[3];
+        for (int m = 0; m < 3; m++) {
+            for (int i = 0; i < 4; i++) w[m][i] = vreinterpretq_u32_u8(vrev32q_u8(vld1q_u8(p[m] + 64 * b + 16 * i)));
+            save0[m] = s0[m];
+            save1[m] = s1[m];
+        }
+        for (int i = 0; i < 16; i++) {
+            const uint32x4_t k = vld1q_u32(K + 4 * i);
+            for (int m = 0; m < 3; m++) {
+                const uint32x4_t wk = vaddq_u32(w[m][i & 3], k);
+                if (i < 12)
+                    w[m][i & 3] = vsha256su1q_u32(vsha256su0q_u32(w[m][i & 3], w[m][(i + 1) & 3]), w[m][(i + 2) & 3],
+                                                  w[m][(i + 3) & 3]);
+                const uint32x4_t abcd = s0[m];
+                s0[m] = vsha256hq_u32(s0[m], s1[m], wk);
+                s1[m] = vsha256h2q_u32(s1[m], abcd, wk);
+            }
+        }
+        for (int m = 0; m < 3; m++) {
+            s0[m] = vaddq_u32(s0[m], save0[m]);
+            s1[m] = vaddq_u32(s1[m], save1[m]);
+        }
+    }
+    for (int m = 0; m < 3; m++) {
+        vst1q_u32(st[m], s0[m]);
+        vst1q_u32(st[m] + 4, s1[m]);
+    }
+}
+#endif
+
+}  // namespace
+
+void sha256_x3(const uint8_t* const in[3], size_t n, uint8_t out[3][32]) {
+#if defined(GKR_SHA_ARMV8)
+    static const uint32_t H0[8] = {0x6a09e667, 0xbb67ae85, 0x3c6ef372, 0xa54ff53a,
+                                   0x510e527f, 0x9b05688c, 0x1f83d9ab, 0x5be0cd19};
+    uint32_t st[3][8];
+    for (int m = 0; m < 3; m++) memcpy(st[m], H0, sizeof(H0));
+    const size_t full = n / 64;
+    compress3(st, in, full);
+    // identical lengths give identical padding: build each tail and finish together
+    const size_t rem = n - 64 * full;
+    const size_t tl = (rem + 9 <= 64) ? 64 : 128;
+    uint8_t tail[3][128];
+    const uint64_t bits = (uint64_t)n * 8;
+    for (int m = 0; m < 3; m++) {
+        memset(tail[m], 0, sizeof(tail[m]));
+        if (rem) memcpy(tail[m], in[m] + 64 * full, rem);
+        tail[m][rem] = 0x80;
+        for (int i = 0; i < 8; i++) tail[m][tl - 1 - i] = (uint8_t)(bits >> (8 * i));
+    }
+    const uint8_t* tp[3] = {tail[0], tail[1], tail[2]};
+    compress3(st, tp, tl / 64);
+    for (int m = 0; m < 3; m++) put_digest(st[m], out[m]);
+#else
+    for (int m = 0; m < 3; m++) sha256(in[m], n, out[m]);
+#endif
+}
+
 const char* sha256_impl_name() {
 #if defined(GKR_SHA_ARMV8)
     return "armv8-sha2";

@@ -24,6 +24,9 @@ struct Sha256 {
 
 void sha256(const uint8_t* in, size_t n, uint8_t out[32]);
 
+// SHA-256 of three messages of the same length (interleaved on ARMv8).
+void sha256_x3(const uint8_t* const in[3], size_t n, uint8_t out[3][32]);
+
 // Name of the compression path compiled in ("armv8-sha2" or "portable").
 const char* sha256_impl_name();
 

@@ -47,6 +47,28 @@ class Transcript {
         has_pre_ = true;
     }
 
+    // Appends three messages of n bytes, each followed by a challenge, exactly as three
+    // append+challenge steps would when nothing else is pending; the three SHA-256 run
+    // interleaved.  Returns false (and does nothing) when bytes are pending.
+    bool append_challenge3(const uint8_t* const msgs[3], uint64_t n, uint32_t out[3]) {
+        if (s_.len != s_.hash_start || has_pre_) return false;
+        const uint8_t* at[3];
+        for (int m = 0; m < 3; m++) {
+            at[m] = buf_ + s_.len;
+            append(msgs[m], n);
+        }
+        uint8_t d[3][32];
+        sha256_x3(at, n, d);
+        s_.hash_start = s_.len;
+        memcpy(s_.digest, d[2], 32);
+        for (int m = 0; m < 3; m++) {
+            uint32_t x;
+            memcpy(&x, d[m], 4);
+            out[m] = m31::from_u32(x);
+        }
+        return true;
+    }
+
     uint32_t challenge() {
         if (has_pre_ && s_.hash_start == pre_from_ && s_.len == pre_to_) {
             memcpy(s_.digest, pre_, 32);
