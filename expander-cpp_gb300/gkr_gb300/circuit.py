@@ -189,6 +189,27 @@ def random_witness(seed, nb_input_vars, n_copies, out=None):
     return res
 
 
+BN254_R = 0x30644E72E131A029B85045B68181585D2833E84879B9709143E1F593F0000001  # BN254 scalar field modulus
+_BN254_TOP = np.uint64(0x30644E72E131A029)
+
+
+def random_witness_bn254(seed, nb_input_vars, n_copies):
+    """BN254 witness of canonical elements, shape (2^nb_input_vars, n_copies, 4) uint64:
+    the 4 little-endian 64-bit limbs of each element (its 32-byte encoding).  The top limb
+    is drawn below r's top limb, so every value is < r."""
+    rows = 1 << nb_input_vars
+    st = Stream(seed ^ 0xB254B254B254B254)
+    limbs = st.u64(rows * n_copies * 4).reshape(rows, n_copies, 4)
+    limbs[..., 3] %= _BN254_TOP
+    return limbs
+
+
+def bn254_values(arr) -> list:
+    """Python integers of a (..., 4) uint64 limb array (flattened)."""
+    a = np.asarray(arr, dtype=np.uint64).reshape(-1, 4)
+    return [int(x[0]) | (int(x[1]) << 64) | (int(x[2]) << 128) | (int(x[3]) << 192) for x in a]
+
+
 def uniform_circuit(seed, depth, width, p_mul=0.5):
     """`depth` layers of 2^width gates with uniform wiring, generated in one vectorised pass
     (the mixed-batch workload builds hundreds of these)."""

@@ -39,7 +39,7 @@ def build_ref(force=False):
         return None
     if os.uname().machine != "x86_64":
         return None
-    srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "build_ref.sh")]
+    srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "build_ref.sh"), os.path.join(HERE, "bn254.h")]
     if not force and not _stale(REF_SO, srcs):
         return REF_SO
     subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT])

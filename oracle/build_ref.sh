@@ -13,7 +13,7 @@ OUT="$HERE/_ref"
 case "$(uname -m)" in x86_64) ;; *) echo "reference build needs x86-64 AVX-512 (this is $(uname -m))" >&2; exit 4;; esac
 mkdir -p "$OUT"
 g++ -std=c++20 -O3 -march=native -mavx512f -mavx512vl -faligned-new -fPIC -shared -w \
-    -DDISABLE_OPTIMIZED_SHA256 \
+    -DDISABLE_OPTIMIZED_SHA256 -DNDEBUG -I"$HERE" \
     -I"$REF/include" -I"$REF/lib" -I"$REF/lib/btc_sha256" \
     "$HERE/ref_driver.cpp" "$REF/lib/btc_sha256/crypto/sha256.cpp" \
     -o "$OUT/libgkr_ref.so.tmp"

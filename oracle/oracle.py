@@ -191,3 +191,80 @@ class Reference:
         out = np.empty(32, np.uint8)
         self.lib.ref_sha256(b.ctypes.data if len(b) else None, len(b), out.ctypes.data)
         return out.tobytes()
+
+
+def _bytes_of(arr):
+    a = np.ascontiguousarray(arr)
+    return a, a.ctypes.data
+
+
+class ReferenceBn254:
+    """The reference prover/verifier templates instantiated with the BN254 type of
+    oracle/bn254.h (x86-64 build only).  Witness: (rows, N, 4) uint64 limbs."""
+
+    def __init__(self, path=None):
+        path = path or _build.REF_SO
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = ctypes.CDLL(path)
+        L = self.lib
+        P, I, U64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64
+        L.ref_prove_bn254.argtypes = [I, P, I, P, I, P, U64, ctypes.POINTER(U64), P]
+        L.ref_verify_bn254.argtypes = [I, P, I, P, I, P, U64, P]
+        L.ref_evaluate_bn254.argtypes = [I, P, I, P, P]
+        L.ref_num_repetitions_bn254.argtypes = [I]
+        for f in ("ref_bn254_mul", "ref_bn254_add", "ref_bn254_sub"):
+            getattr(L, f).argtypes = [P, P, P]
+        L.ref_bn254_reduce.argtypes = [P, P]
+        sup = (ctypes.c_int * 5).in_dll(L, "ref_supported_lanes_bn254")
+        self.supported_lanes = [v for v in sup if v]
+
+    @staticmethod
+    def proof_size(circuit, n_copies):
+        rows = sum(6 * l.nb_input_vars + 2 for l in circuit.layers)
+        return (1 << circuit.layers[0].nb_input_vars) * n_copies * 32 + 32 + rows * n_copies * 32
+
+    def prove(self, circuit, witness, grinding_bits=10):
+        w, wp = _bytes_of(np.asarray(witness, dtype=np.uint64))
+        N = w.shape[1]
+        cap = self.proof_size(circuit, N)
+        proof = np.empty(cap, np.uint8)
+        cv = np.empty((1, N, 4), np.uint64)
+        plen = ctypes.c_uint64()
+        arr, keep = _layers(circuit)
+        rc = self.lib.ref_prove_bn254(N, arr, len(circuit.layers), wp, grinding_bits, proof.ctypes.data, cap,
+                                      ctypes.byref(plen), cv.ctypes.data)
+        if rc != 0:
+            raise ValueError(f"ref_prove_bn254 failed rc={rc}")
+        return cv, proof[:plen.value].tobytes()
+
+    def verify(self, circuit, witness, claimed_v, proof, grinding_bits=10):
+        w, wp = _bytes_of(np.asarray(witness, dtype=np.uint64))
+        cv, cvp = _bytes_of(np.asarray(claimed_v, dtype=np.uint64))
+        pb = np.frombuffer(bytes(proof), np.uint8)
+        arr, keep = _layers(circuit)
+        rc = self.lib.ref_verify_bn254(w.shape[1], arr, len(circuit.layers), wp, grinding_bits, pb.ctypes.data,
+                                       len(pb), cvp)
+        if rc < 0:
+            raise ValueError("ref_verify_bn254: unsupported lanes")
+        return rc == 1
+
+    def evaluate(self, circuit, witness):
+        w, wp = _bytes_of(np.asarray(witness, dtype=np.uint64))
+        N = w.shape[1]
+        sizes = [1 << l.nb_input_vars for l in circuit.layers] + [1 << circuit.layers[-1].nb_output_vars]
+        out = np.empty((sum(sizes), N, 4), np.uint64)
+        arr, keep = _layers(circuit)
+        if self.lib.ref_evaluate_bn254(N, arr, len(circuit.layers), wp, out.ctypes.data) != 0:
+            raise ValueError("ref_evaluate_bn254: unsupported lanes")
+        return np.split(out, np.cumsum(sizes)[:-1])
+
+    def field_op(self, name, a: int, b: int = 0) -> int:
+        ab = a.to_bytes(32, "little")
+        bb = b.to_bytes(32, "little")
+        out = ctypes.create_string_buffer(32)
+        if name == "reduce":
+            self.lib.ref_bn254_reduce(ab, out)
+        else:
+            getattr(self.lib, "ref_bn254_" + name)(ab, bb, out)
+        return int.from_bytes(out.raw, "little")

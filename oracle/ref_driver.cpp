@@ -6,9 +6,18 @@
 //
 // The reference packs 8 circuit copies per field element on x86 (VectorizedM31,
 // include/field/M31.hpp:240-449).  To run its templates with other copy counts this
-// driver supplies LaneVec<N>, an N-lane element whose arithmetic calls the reference's
-// own scalar M31 operators (include/field/M31.hpp:64-93).  At N=8 the proofs of
-// LaneVec<8> and of VectorizedM31 are compared byte for byte by the tests.
+// driver supplies LaneVec<E, N>, an N-lane element whose arithmetic calls the scalar type
+// E's operators: the reference's own M31 (include/field/M31.hpp:64-93), or Bn254 below.
+// At N=8 the proofs of LaneVec<M31, 8> and of VectorizedM31 are compared byte for byte by
+// the tests.
+//
+// BN254: the reference declares the field (include/configuration/config.hpp:12-16,53-55)
+// but its implementation header is missing, so Bn254 here is this project's definition
+// (oracle/bn254.h: canonical 32-byte little-endian encoding, from_bytes reduces mod r).
+// Instantiating the reference templates with it pins the protocol (transcript schedule,
+// grinding with one 32-byte challenge, R = 1) for the BN254 prover.  The reference's
+// Prover constructor asserts M31 (include/LinearGKR/LinearGKR.hpp:44), so this driver is
+// compiled with NDEBUG.
 //
 // Everything the reference headers define must live in exactly one translation unit
 // (include/field/M31.hpp:451-452 and include/utils/myutil.hpp define non-inline symbols).
@@ -19,39 +28,75 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
-#include <unistd.h>
 #include <fcntl.h>
+#include <unistd.h>
+
+#include "bn254.h"
 
 namespace refdrv {
 
 using gkr::M31_field::M31;
 static const uint32_t P = 2147483647u;
 
-template <int N>
-struct Lanes {
-    uint32_t v[N];
-    static uint32_t ladd(uint32_t a, uint32_t b) { return (M31::new_unchecked(a) + M31::new_unchecked(b)).x; }
-    static uint32_t lsub(uint32_t a, uint32_t b) { return (M31::new_unchecked(a) - M31::new_unchecked(b)).x; }
-    static uint32_t lmul(uint32_t a, uint32_t b) { return (M31::new_unchecked(a) * M31::new_unchecked(b)).x; }
-    Lanes operator+(const Lanes& o) const { Lanes r; for (int i = 0; i < N; i++) r.v[i] = ladd(v[i], o.v[i]); return r; }
-    Lanes operator-(const Lanes& o) const { Lanes r; for (int i = 0; i < N; i++) r.v[i] = lsub(v[i], o.v[i]); return r; }
-    Lanes operator*(const Lanes& o) const { Lanes r; for (int i = 0; i < N; i++) r.v[i] = lmul(v[i], o.v[i]); return r; }
-    Lanes operator*(const M31& s) const { Lanes r; for (int i = 0; i < N; i++) r.v[i] = lmul(v[i], s.x); return r; }
-    void operator+=(const Lanes& o) { *this = *this + o; }
-    bool operator==(const Lanes& o) const { return memcmp(v, o.v, sizeof(v)) == 0; }
+// BN254 scalar with the interface the reference templates use for F_primitive.
+struct Bn254 {
+    bn_t a;
+    static Bn254 INV_2;
+    Bn254() { memset(a.v, 0, 32); }
+    Bn254(uint32_t x) { a = bn_from_u32(x); }
+    static Bn254 mk(bn_t v) { Bn254 r; r.a = v; return r; }
+    static Bn254 zero() { return Bn254(); }
+    static Bn254 one() { return Bn254(1u); }
+    Bn254 operator+(const Bn254& o) const { return mk(bn_add(a, o.a)); }
+    Bn254 operator-(const Bn254& o) const { return mk(bn_sub(a, o.a)); }
+    Bn254 operator-() const { return mk(bn_neg(a)); }
+    Bn254 operator*(const Bn254& o) const { return mk(bn_mul(a, o.a)); }
+    void operator+=(const Bn254& o) { a = bn_add(a, o.a); }
+    void operator-=(const Bn254& o) { a = bn_sub(a, o.a); }
+    void operator*=(const Bn254& o) { a = bn_mul(a, o.a); }
+    bool operator==(const Bn254& o) const { return bn_eq(a, o.a); }
+    void to_bytes(uint8_t* out) const { bn_to_bytes(a, out); }
+    void from_bytes(const uint8_t* in) { a = bn_from_bytes(in); }
+    static int byte_length() { return 32; }
+};
+Bn254 Bn254::INV_2 = Bn254::mk(bn_t{{0xa1f0fac9f8000001ull, 0x9419f4243cdcb848ull, 0xdc2822db40c0ac2eull,
+                                      0x183227397098d014ull}});
+
+template <class E> struct Elem;
+template <> struct Elem<M31> {
+    static constexpr int bytes = 4;
+    static M31 make(uint32_t x) { M31 m(x); if (m.x >= P) m.x -= P; return m; }
+    static M31 inv2() { return M31::new_unchecked(1u << 30); }
+};
+template <> struct Elem<Bn254> {
+    static constexpr int bytes = 32;
+    static Bn254 make(uint32_t x) { return Bn254(x); }
+    static Bn254 inv2() { return Bn254::INV_2; }
 };
 
-// N-lane stand-in for VectorizedM31: one Lanes<N> "packed" element, because the
-// reference indexes .elements[j] for j < vectorize_size (== 1 on x86),
+template <class E, int N>
+struct Lanes {
+    E v[N];
+    Lanes operator+(const Lanes& o) const { Lanes r; for (int i = 0; i < N; i++) r.v[i] = v[i] + o.v[i]; return r; }
+    Lanes operator-(const Lanes& o) const { Lanes r; for (int i = 0; i < N; i++) r.v[i] = v[i] - o.v[i]; return r; }
+    Lanes operator*(const Lanes& o) const { Lanes r; for (int i = 0; i < N; i++) r.v[i] = v[i] * o.v[i]; return r; }
+    Lanes operator*(const E& s) const { Lanes r; for (int i = 0; i < N; i++) r.v[i] = v[i] * s; return r; }
+    void operator+=(const Lanes& o) { *this = *this + o; }
+    bool operator==(const Lanes& o) const { for (int i = 0; i < N; i++) if (!(v[i] == o.v[i])) return false; return true; }
+};
+
+// N-lane stand-in for VectorizedM31: one Lanes "packed" element, because the reference
+// indexes .elements[j] for j < vectorize_size (== 1 on x86),
 // include/LinearGKR/sumcheck_helper.hpp:82-97,113-126.
-template <int N>
+template <class E, int N>
 struct LaneVec {
-    typedef M31 primitive_type;
-    Lanes<N> elements[1];
+    typedef E primitive_type;
+    Lanes<E, N> elements[1];
     static LaneVec INV_2;
 
-    LaneVec() { memset(elements[0].v, 0, sizeof(elements[0].v)); }
-    LaneVec(uint32_t x) { M31 m(x); if (m.x >= P) m.x -= P; for (int i = 0; i < N; i++) elements[0].v[i] = m.x; }
+    LaneVec() { for (int i = 0; i < N; i++) elements[0].v[i] = E(); }
+    LaneVec(uint32_t x) { const E e = Elem<E>::make(x); for (int i = 0; i < N; i++) elements[0].v[i] = e; }
+    static LaneVec bcast(const E& e) { LaneVec r; for (int i = 0; i < N; i++) r.elements[0].v[i] = e; return r; }
     static LaneVec zero() { return LaneVec(); }
     static LaneVec one() { return LaneVec(1u); }
     static size_t pack_size() { return N; }
@@ -60,28 +105,20 @@ struct LaneVec {
     LaneVec operator-(const LaneVec& o) const { LaneVec r; r.elements[0] = elements[0] - o.elements[0]; return r; }
     LaneVec operator-() const { return LaneVec() - *this; }
     LaneVec operator*(const LaneVec& o) const { LaneVec r; r.elements[0] = elements[0] * o.elements[0]; return r; }
-    LaneVec operator*(const M31& s) const { LaneVec r; r.elements[0] = elements[0] * s; return r; }
+    LaneVec operator*(const E& s) const { LaneVec r; r.elements[0] = elements[0] * s; return r; }
     LaneVec operator*(const int& s) const { return *this * LaneVec((uint32_t)s); }
-    LaneVec operator+(const M31& s) const { return *this + LaneVec(s.x); }
+    LaneVec operator+(const E& s) const { return *this + bcast(s); }
     void operator+=(const LaneVec& o) { *this = *this + o; }
     void operator-=(const LaneVec& o) { *this = *this - o; }
     void operator*=(const LaneVec& o) { *this = *this * o; }
     bool operator==(const LaneVec& o) const { return elements[0] == o.elements[0]; }
 
     // Same byte layout as VectorizedM31::to_bytes/from_bytes (M31.hpp:420-434,
-    // M31_avx.tcc:62-67): N little-endian u32 lanes, reduced on read.
-    void to_bytes(uint8_t* out) const { memcpy(out, elements[0].v, 4 * N); }
-    void from_bytes(const uint8_t* in) {
-        memcpy(elements[0].v, in, 4 * N);
-        for (int i = 0; i < N; i++) {
-            uint32_t x = elements[0].v[i];
-            x = (x & P) + (x >> 31);
-            if (x >= P) x -= P;
-            elements[0].v[i] = x;
-        }
-    }
+    // M31_avx.tcc:62-67): N elements in lane order, each reduced on read.
+    void to_bytes(uint8_t* out) const { for (int i = 0; i < N; i++) elements[0].v[i].to_bytes(out + i * Elem<E>::bytes); }
+    void from_bytes(const uint8_t* in) { for (int i = 0; i < N; i++) elements[0].v[i].from_bytes(in + i * Elem<E>::bytes); }
 };
-template <int N> LaneVec<N> LaneVec<N>::INV_2 = LaneVec<N>(1u << 30);
+template <class E, int N> LaneVec<E, N> LaneVec<E, N>::INV_2 = LaneVec<E, N>::bcast(Elem<E>::inv2());
 
 }  // namespace refdrv
 
@@ -99,9 +136,9 @@ struct ref_layer {
 
 namespace refdrv {
 
-template <class F>
-static gkr::Circuit<F, M31> build_circuit(const ref_layer* layers, int nlayers, const uint32_t* input, int lanes) {
-    gkr::Circuit<F, M31> c;
+template <class F, class Fp>
+static gkr::Circuit<F, Fp> build_circuit(const ref_layer* layers, int nlayers, const uint8_t* input, size_t row_bytes) {
+    gkr::Circuit<F, Fp> c;
     c.layers.resize(nlayers);
     for (int l = 0; l < nlayers; l++) {
         auto& L = c.layers[l];
@@ -114,26 +151,27 @@ static gkr::Circuit<F, M31> build_circuit(const ref_layer* layers, int nlayers, 
         for (uint64_t g = 0; g < layers[l].n_mul; g++) {
             const uint32_t* s = layers[l].mul + 4 * g;
             auto& G = L.mul.sparse_evals[g];
-            G.o_id = s[0]; G.i_ids[0] = s[1]; G.i_ids[1] = s[2]; G.coef = M31(s[3]);
+            G.o_id = s[0]; G.i_ids[0] = s[1]; G.i_ids[1] = s[2]; G.coef = Fp(s[3]);
         }
         L.add.sparse_evals.resize(layers[l].n_add);
         for (uint64_t g = 0; g < layers[l].n_add; g++) {
             const uint32_t* s = layers[l].add + 3 * g;
             auto& G = L.add.sparse_evals[g];
-            G.o_id = s[0]; G.i_ids[0] = s[1]; G.coef = M31(s[2]);
+            G.o_id = s[0]; G.i_ids[0] = s[1]; G.coef = Fp(s[2]);
         }
     }
     uint64_t I0 = 1ull << layers[0].nb_input_vars;
     auto& ev = c.layers[0].input_layer_vals.evals;
     ev.resize(I0);
-    for (uint64_t i = 0; i < I0; i++) ev[i].from_bytes((const uint8_t*)(input + i * lanes));
+    for (uint64_t i = 0; i < I0; i++) ev[i].from_bytes(input + i * row_bytes);
     c.evaluate();
     return c;
 }
 
-static ::Config make_config(int grinding_bits) {
+static ::Config make_config(int grinding_bits, bool bn254 = false) {
     ::Config cfg;
     cfg.grinding_bits = grinding_bits;
+    if (bn254) cfg.field_type = Field_type::BN254;
     cfg.initialize_config();
     return cfg;
 }
@@ -145,12 +183,12 @@ struct Mute {
     ~Mute() { fflush(stdout); std::cout.flush(); dup2(saved, 1); close(saved); }
 };
 
-template <class F>
-static int prove_t(const ref_layer* layers, int nlayers, int lanes, const uint32_t* input, int grinding_bits,
-                   uint8_t* proof_out, uint64_t proof_cap, uint64_t* proof_len, uint32_t* claimed_v) {
-    auto circuit = build_circuit<F>(layers, nlayers, input, lanes);
-    ::Config cfg = make_config(grinding_bits);
-    gkr::Prover<F, M31> prover(cfg);
+template <class F, class Fp>
+static int prove_t(const ref_layer* layers, int nlayers, const uint8_t* input, size_t row_bytes, int grinding_bits,
+                   bool bn254, uint8_t* proof_out, uint64_t proof_cap, uint64_t* proof_len, uint8_t* claimed_v) {
+    auto circuit = build_circuit<F, Fp>(layers, nlayers, input, row_bytes);
+    ::Config cfg = make_config(grinding_bits, bn254);
+    gkr::Prover<F, Fp> prover(cfg);
     prover.prepare_mem(circuit);
     auto t = prover.prove(circuit);
     auto& cv = std::get<0>(t);
@@ -158,19 +196,19 @@ static int prove_t(const ref_layer* layers, int nlayers, int lanes, const uint32
     *proof_len = proof.bytes.size();
     if (proof.bytes.size() > proof_cap) return 2;
     memcpy(proof_out, proof.bytes.data(), proof.bytes.size());
-    for (size_t j = 0; j < cv.size(); j++) cv[j].to_bytes((uint8_t*)(claimed_v + j * lanes));
+    for (size_t j = 0; j < cv.size(); j++) cv[j].to_bytes(claimed_v + j * row_bytes);
     return 0;
 }
 
-template <class F>
-static int verify_t(const ref_layer* layers, int nlayers, int lanes, const uint32_t* input, int grinding_bits,
-                    const uint8_t* proof_bytes, uint64_t proof_len, const uint32_t* claimed_v) {
-    auto circuit = build_circuit<F>(layers, nlayers, input, lanes);
-    ::Config cfg = make_config(grinding_bits);
+template <class F, class Fp>
+static int verify_t(const ref_layer* layers, int nlayers, const uint8_t* input, size_t row_bytes, int grinding_bits,
+                    bool bn254, const uint8_t* proof_bytes, uint64_t proof_len, const uint8_t* claimed_v) {
+    auto circuit = build_circuit<F, Fp>(layers, nlayers, input, row_bytes);
+    ::Config cfg = make_config(grinding_bits, bn254);
     gkr::Proof<F> proof;
     proof.bytes.assign(proof_bytes, proof_bytes + proof_len);
     std::vector<F> cv(cfg.get_num_repetitions());
-    for (int j = 0; j < cfg.get_num_repetitions(); j++) cv[j].from_bytes((const uint8_t*)(claimed_v + (size_t)j * lanes));
+    for (int j = 0; j < cfg.get_num_repetitions(); j++) cv[j].from_bytes(claimed_v + (size_t)j * row_bytes);
     gkr::Verifier verifier(cfg);
     bool ok;
     {
@@ -180,38 +218,51 @@ static int verify_t(const ref_layer* layers, int nlayers, int lanes, const uint3
     return ok ? 1 : 0;
 }
 
-template <class F>
-static int evaluate_t(const ref_layer* layers, int nlayers, int lanes, const uint32_t* input, uint32_t* out) {
-    auto circuit = build_circuit<F>(layers, nlayers, input, lanes);
+template <class F, class Fp>
+static int evaluate_t(const ref_layer* layers, int nlayers, const uint8_t* input, size_t row_bytes, uint8_t* out) {
+    auto circuit = build_circuit<F, Fp>(layers, nlayers, input, row_bytes);
     uint64_t off = 0;
     for (int l = 0; l < nlayers; l++) {
-        for (auto& e : circuit.layers[l].input_layer_vals.evals) { e.to_bytes((uint8_t*)(out + off)); off += lanes; }
+        for (auto& e : circuit.layers[l].input_layer_vals.evals) { e.to_bytes(out + off); off += row_bytes; }
     }
-    for (auto& e : circuit.layers.back().output_layer_vals.evals) { e.to_bytes((uint8_t*)(out + off)); off += lanes; }
+    for (auto& e : circuit.layers.back().output_layer_vals.evals) { e.to_bytes(out + off); off += row_bytes; }
     return 0;
 }
 
+template <int N> using M31L = LaneVec<M31, N>;
+template <int N> using BnL = LaneVec<Bn254, N>;
+
 }  // namespace refdrv
 
-#define REF_DISPATCH(FN, ...)                                                              \
-    switch (lanes) {                                                                       \
-        case 4: return refdrv::FN<refdrv::LaneVec<4>>(__VA_ARGS__);                        \
-        case 8: return native ? refdrv::FN<gkr::M31_field::VectorizedM31>(__VA_ARGS__)     \
-                              : refdrv::FN<refdrv::LaneVec<8>>(__VA_ARGS__);               \
-        case 16: return refdrv::FN<refdrv::LaneVec<16>>(__VA_ARGS__);                      \
-        case 32: return refdrv::FN<refdrv::LaneVec<32>>(__VA_ARGS__);                      \
-        case 48: return refdrv::FN<refdrv::LaneVec<48>>(__VA_ARGS__);                      \
-        case 64: return refdrv::FN<refdrv::LaneVec<64>>(__VA_ARGS__);                      \
-        case 128: return refdrv::FN<refdrv::LaneVec<128>>(__VA_ARGS__);                    \
-        case 256: return refdrv::FN<refdrv::LaneVec<256>>(__VA_ARGS__);                    \
-        case 1024: return refdrv::FN<refdrv::LaneVec<1024>>(__VA_ARGS__);                  \
-        default: return -1;                                                                \
+#define REF_M31(FN, ...)                                                                          \
+    switch (lanes) {                                                                              \
+        case 4: return refdrv::FN<refdrv::M31L<4>, refdrv::M31>(__VA_ARGS__);                     \
+        case 8: return native ? refdrv::FN<gkr::M31_field::VectorizedM31, refdrv::M31>(__VA_ARGS__) \
+                              : refdrv::FN<refdrv::M31L<8>, refdrv::M31>(__VA_ARGS__);            \
+        case 16: return refdrv::FN<refdrv::M31L<16>, refdrv::M31>(__VA_ARGS__);                   \
+        case 32: return refdrv::FN<refdrv::M31L<32>, refdrv::M31>(__VA_ARGS__);                   \
+        case 48: return refdrv::FN<refdrv::M31L<48>, refdrv::M31>(__VA_ARGS__);                   \
+        case 64: return refdrv::FN<refdrv::M31L<64>, refdrv::M31>(__VA_ARGS__);                   \
+        case 128: return refdrv::FN<refdrv::M31L<128>, refdrv::M31>(__VA_ARGS__);                 \
+        case 256: return refdrv::FN<refdrv::M31L<256>, refdrv::M31>(__VA_ARGS__);                 \
+        case 1024: return refdrv::FN<refdrv::M31L<1024>, refdrv::M31>(__VA_ARGS__);               \
+        default: return -1;                                                                       \
+    }
+
+#define REF_BN(FN, ...)                                                        \
+    switch (lanes) {                                                           \
+        case 4: return refdrv::FN<refdrv::BnL<4>, refdrv::Bn254>(__VA_ARGS__);   \
+        case 8: return refdrv::FN<refdrv::BnL<8>, refdrv::Bn254>(__VA_ARGS__);   \
+        case 16: return refdrv::FN<refdrv::BnL<16>, refdrv::Bn254>(__VA_ARGS__); \
+        case 64: return refdrv::FN<refdrv::BnL<64>, refdrv::Bn254>(__VA_ARGS__); \
+        default: return -1;                                                    \
     }
 
 extern "C" {
 
 // Lane counts this driver was instantiated for (0-terminated).
 extern const int ref_supported_lanes[] = {4, 8, 16, 32, 48, 64, 128, 256, 1024, 0};
+extern const int ref_supported_lanes_bn254[] = {4, 8, 16, 64, 0};
 
 int ref_num_repetitions(int grinding_bits) { return refdrv::make_config(grinding_bits).get_num_repetitions(); }
 
@@ -221,19 +272,51 @@ int ref_num_repetitions(int grinding_bits) { return refdrv::make_config(grinding
 // unsupported lane count, 2 if proof_cap is too small (proof_len is still set).
 int ref_prove(int lanes, int native, const ref_layer* layers, int nlayers, const uint32_t* input, int grinding_bits,
               uint8_t* proof_out, uint64_t proof_cap, uint64_t* proof_len, uint32_t* claimed_v) {
-    REF_DISPATCH(prove_t, layers, nlayers, lanes, input, grinding_bits, proof_out, proof_cap, proof_len, claimed_v)
+    REF_M31(prove_t, layers, nlayers, (const uint8_t*)input, (size_t)lanes * 4, grinding_bits, false, proof_out,
+            proof_cap, proof_len, (uint8_t*)claimed_v)
 }
 
 // Verifier::verify (include/LinearGKR/LinearGKR.hpp:105-149).  Returns 1 accept, 0 reject.
 int ref_verify(int lanes, int native, const ref_layer* layers, int nlayers, const uint32_t* input, int grinding_bits,
                const uint8_t* proof, uint64_t proof_len, const uint32_t* claimed_v) {
-    REF_DISPATCH(verify_t, layers, nlayers, lanes, input, grinding_bits, proof, proof_len, claimed_v)
+    REF_M31(verify_t, layers, nlayers, (const uint8_t*)input, (size_t)lanes * 4, grinding_bits, false, proof,
+            proof_len, (const uint8_t*)claimed_v)
 }
 
 // Circuit::evaluate: writes every layer's input values followed by the last layer's output.
 int ref_evaluate(int lanes, int native, const ref_layer* layers, int nlayers, const uint32_t* input, uint32_t* out) {
-    REF_DISPATCH(evaluate_t, layers, nlayers, lanes, input, out)
+    REF_M31(evaluate_t, layers, nlayers, (const uint8_t*)input, (size_t)lanes * 4, (uint8_t*)out)
 }
+
+// The same three entry points over BN254 (Config::field_type = BN254: R = 1): values are
+// rows of `lanes` 32-byte little-endian canonical elements.
+int ref_prove_bn254(int lanes, const ref_layer* layers, int nlayers, const uint8_t* input, int grinding_bits,
+                    uint8_t* proof_out, uint64_t proof_cap, uint64_t* proof_len, uint8_t* claimed_v) {
+    REF_BN(prove_t, layers, nlayers, input, (size_t)lanes * 32, grinding_bits, true, proof_out, proof_cap, proof_len,
+           claimed_v)
+}
+int ref_verify_bn254(int lanes, const ref_layer* layers, int nlayers, const uint8_t* input, int grinding_bits,
+                     const uint8_t* proof, uint64_t proof_len, const uint8_t* claimed_v) {
+    REF_BN(verify_t, layers, nlayers, input, (size_t)lanes * 32, grinding_bits, true, proof, proof_len, claimed_v)
+}
+int ref_evaluate_bn254(int lanes, const ref_layer* layers, int nlayers, const uint8_t* input, uint8_t* out) {
+    REF_BN(evaluate_t, layers, nlayers, input, (size_t)lanes * 32, out)
+}
+int ref_num_repetitions_bn254(int grinding_bits) {
+    return refdrv::make_config(grinding_bits, true).get_num_repetitions();
+}
+
+// BN254 field helpers for the tests (canonical 32-byte little-endian values).
+void ref_bn254_mul(const uint8_t* a, const uint8_t* b, uint8_t* out) {
+    bn_to_bytes(bn_mul(bn_from_bytes(a), bn_from_bytes(b)), out);
+}
+void ref_bn254_add(const uint8_t* a, const uint8_t* b, uint8_t* out) {
+    bn_to_bytes(bn_add(bn_from_bytes(a), bn_from_bytes(b)), out);
+}
+void ref_bn254_sub(const uint8_t* a, const uint8_t* b, uint8_t* out) {
+    bn_to_bytes(bn_sub(bn_from_bytes(a), bn_from_bytes(b)), out);
+}
+void ref_bn254_reduce(const uint8_t* a, uint8_t* out) { bn_to_bytes(bn_from_bytes(a), out); }
 
 // SHA256Hasher::hash (include/hash/hashes.hpp:22-33) -> CSHA256.
 void ref_sha256(const uint8_t* in, uint64_t len, uint8_t* out) {
