@@ -25,7 +25,11 @@ namespace gkrgpu {
 
 const char* const kKernelNames[K_NUM_KERNELS] = {"check_canonical", "evaluate", "eq_table", "gate_weights",
                                                  "hg_build_round0", "round_fold_lane", "round_fold_scalar",
-                                                 "phase2_s_build", "weighted_row_sum"};
+                                                 "phase2_s_build", "weighted_row_sum", "bn254_load",
+                                                 "bn254_evaluate", "bn254_eq_table", "bn254_gate_weights",
+                                                 "bn254_hg_build_round0", "bn254_round_fold_lane",
+                                                 "bn254_round_fold_scalar", "bn254_phase2_s_build",
+                                                 "bn254_weighted_row_sum", "bn254_unload"};
 
 namespace {
 

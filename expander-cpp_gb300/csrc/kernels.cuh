@@ -57,6 +57,17 @@ enum KernelId {
     K_ROUND_SCALAR,
     K_S_BUILD,
     K_WSUM,
+    // BN254 kernels (bn254.cuh)
+    K_BN_LOAD,
+    K_BN_EVALUATE,
+    K_BN_EQ,
+    K_BN_WEIGHTS,
+    K_BN_HG_ROUND0,
+    K_BN_ROUND_LANE,
+    K_BN_ROUND_SCALAR,
+    K_BN_S_BUILD,
+    K_BN_WSUM,
+    K_BN_UNLOAD,
     K_NUM_KERNELS
 };
 extern const char* const kKernelNames[K_NUM_KERNELS];

@@ -38,6 +38,8 @@
 #include <vector>
 
 #include "../../include/gkrgpu.h"
+#include "bn254.cuh"
+#include "fr_host.hpp"
 #include "kernels.cuh"
 #include "m31.cuh"
 #include "sha256.hpp"
@@ -92,6 +94,18 @@ int reps_for(int grinding_bits) {
     const int s = 100 - grinding_bits;
     return s / 31 + (s % 31 != 0);
 }
+
+// The same for a field of `field_size` bits (254 for BN254).
+int reps_for_field(int field, int grinding_bits) {
+    if (field != GKRGPU_FIELD_BN254) return reps_for(grinding_bits);
+    const int s = 100 - grinding_bits;
+    return s / 254 + (s % 254 != 0);
+}
+
+bool field_supported(int field) { return field == GKRGPU_FIELD_M31 || field == GKRGPU_FIELD_BN254; }
+
+// Bytes of one field element: M31 4, BN254 32.
+uint32_t elem_bytes(int field) { return field == GKRGPU_FIELD_BN254 ? 32u : 4u; }
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -150,11 +164,14 @@ struct DevLayer {
     // phase two: mul gates grouped by y = i1
     uint32_t* my_off = nullptr;  // I+1
     uint4* my_g = nullptr;       // (x, z, c, 0)
+    // BN254 circuits: each gate's coefficient in Montgomery form, in the order of the table above
+    const bn::Fr *mo_c = nullptr, *ao_c = nullptr, *mx_c = nullptr, *ax_c = nullptr, *my_c = nullptr;
     void* block = nullptr;
 };
 
 struct gkrgpu_circuit {
     int device = 0;
+    int field = GKRGPU_FIELD_M31;
     std::vector<DevLayer> layers;
     uint32_t max_in_vars = 0, max_out_vars = 0;
     uint64_t max_mul = 0;
@@ -462,12 +479,26 @@ void csr(uint64_t nkeys, uint64_t n, const std::vector<uint32_t>& keys, std::vec
     for (uint64_t i = 0; i < n; i++) order[pos[keys[i]]++] = (uint32_t)i;
 }
 
-DevLayer upload_layer(const gkrgpu_layer_desc& d) {
+DevLayer upload_layer(const gkrgpu_layer_desc& d, int field) {
     const uint64_t I = 1ull << d.nb_input_vars, O = 1ull << d.nb_output_vars;
     const uint64_t Gm = d.n_mul, Ga = d.n_add;
+    const bool bn = field == GKRGPU_FIELD_BN254;
     std::vector<uint32_t> keys, off_mo, off_ao, off_mx, off_ax, off_my, ord;
     std::vector<uint4> mo(Gm), mx(Gm), my(Gm);
     std::vector<uint2> ao(Ga), ax(Ga);
+    // BN254: Montgomery coefficients per gate, then permuted into each table's order
+    std::vector<frh::Fr> cm, ca, mo_c, mx_c, my_c, ao_c, ax_c;
+    if (bn) {
+        cm.resize(Gm);
+        ca.resize(Ga);
+        for (uint64_t i = 0; i < Gm; i++) cm[i] = frh::to_mont(frh::from_u32(d.mul[i].coef));
+        for (uint64_t i = 0; i < Ga; i++) ca[i] = frh::to_mont(frh::from_u32(d.add[i].coef));
+        mo_c.resize(Gm);
+        mx_c.resize(Gm);
+        my_c.resize(Gm);
+        ao_c.resize(Ga);
+        ax_c.resize(Ga);
+    }
 
     keys.resize(Gm);
     for (uint64_t i = 0; i < Gm; i++) keys[i] = d.mul[i].o_id;
@@ -475,18 +506,21 @@ DevLayer upload_layer(const gkrgpu_layer_desc& d) {
     for (uint64_t k = 0; k < Gm; k++) {
         const auto& g = d.mul[ord[k]];
         mo[k] = make_uint4(g.i0, g.i1, g.coef, 0);
+        if (bn) mo_c[k] = cm[ord[k]];
     }
     for (uint64_t i = 0; i < Gm; i++) keys[i] = d.mul[i].i0;
     csr(I, Gm, keys, off_mx, ord);
     for (uint64_t k = 0; k < Gm; k++) {
         const auto& g = d.mul[ord[k]];
         mx[k] = make_uint4(g.i1, g.o_id, g.coef, 0);
+        if (bn) mx_c[k] = cm[ord[k]];
     }
     for (uint64_t i = 0; i < Gm; i++) keys[i] = d.mul[i].i1;
     csr(I, Gm, keys, off_my, ord);
     for (uint64_t k = 0; k < Gm; k++) {
         const auto& g = d.mul[ord[k]];
         my[k] = make_uint4(g.i0, g.o_id, g.coef, 0);
+        if (bn) my_c[k] = cm[ord[k]];
     }
     keys.resize(Ga);
     for (uint64_t i = 0; i < Ga; i++) keys[i] = d.add[i].o_id;
@@ -494,12 +528,14 @@ DevLayer upload_layer(const gkrgpu_layer_desc& d) {
     for (uint64_t k = 0; k < Ga; k++) {
         const auto& g = d.add[ord[k]];
         ao[k] = make_uint2(g.i0, g.coef);
+        if (bn) ao_c[k] = ca[ord[k]];
     }
     for (uint64_t i = 0; i < Ga; i++) keys[i] = d.add[i].i0;
     csr(I, Ga, keys, off_ax, ord);
     for (uint64_t k = 0; k < Ga; k++) {
         const auto& g = d.add[ord[k]];
         ax[k] = make_uint2(g.o_id, g.coef);
+        if (bn) ax_c[k] = ca[ord[k]];
     }
 
     struct Part {
@@ -519,6 +555,13 @@ DevLayer upload_layer(const gkrgpu_layer_desc& d) {
         {off_ax.data(), off_ax.size() * 4, (void**)&L.ax_off}, {ax.data(), Ga * 8, (void**)&L.ax_g},
         {off_my.data(), off_my.size() * 4, (void**)&L.my_off}, {my.data(), Gm * 16, (void**)&L.my_g},
     };
+    if (bn) {
+        parts.push_back({mo_c.data(), Gm * 32, (void**)&L.mo_c});
+        parts.push_back({ao_c.data(), Ga * 32, (void**)&L.ao_c});
+        parts.push_back({mx_c.data(), Gm * 32, (void**)&L.mx_c});
+        parts.push_back({ax_c.data(), Ga * 32, (void**)&L.ax_c});
+        parts.push_back({my_c.data(), Gm * 32, (void**)&L.my_c});
+    }
     size_t total = 0;
     for (auto& p : parts) total += align_up(std::max<size_t>(p.bytes, 16), 256);
     cudaError_t e = cudaMalloc(&L.block, total);
@@ -541,7 +584,10 @@ DevLayer upload_layer(const gkrgpu_layer_desc& d) {
     return L;
 }
 
-void validate_layers(const gkrgpu_layer_desc* layers, int n) {
+void validate_layers(const gkrgpu_layer_desc* layers, int n, int field) {
+    if (!field_supported(field)) fail(GKRGPU_ERR_INVALID, "unsupported field type %d (M31 = 0, BN254 = 2)", field);
+    // every u32 coefficient is a canonical BN254 element; M31 coefficients must be below p
+    const uint32_t coef_limit = field == GKRGPU_FIELD_BN254 ? 0xffffffffu : m31::P - 1;
     if (!layers || n <= 0) fail(GKRGPU_ERR_INVALID, "circuit needs at least one layer");
     for (int l = 0; l < n; l++) {
         const auto& d = layers[l];
@@ -555,12 +601,12 @@ void validate_layers(const gkrgpu_layer_desc* layers, int n) {
         const uint64_t I = 1ull << d.nb_input_vars, O = 1ull << d.nb_output_vars;
         for (uint64_t g = 0; g < d.n_mul; g++) {
             const auto& m = d.mul[g];
-            if (m.o_id >= O || m.i0 >= I || m.i1 >= I || m.coef >= m31::P)
+            if (m.o_id >= O || m.i0 >= I || m.i1 >= I || m.coef > coef_limit)
                 fail(GKRGPU_ERR_INVALID, "layer %d mul gate %llu: id or coefficient out of range", l, (unsigned long long)g);
         }
         for (uint64_t g = 0; g < d.n_add; g++) {
             const auto& a = d.add[g];
-            if (a.o_id >= O || a.i0 >= I || a.coef >= m31::P)
+            if (a.o_id >= O || a.i0 >= I || a.coef > coef_limit)
                 fail(GKRGPU_ERR_INVALID, "layer %d add gate %llu: id or coefficient out of range", l, (unsigned long long)g);
         }
     }
@@ -938,6 +984,8 @@ struct Prover {
     }
 };
 
+#include "bn254_prover.cuh"
+
 void check_ctx(gkrgpu_ctx* ctx) {
     if (!ctx) fail(GKRGPU_ERR_INVALID, "null context");
 }
@@ -946,20 +994,30 @@ void check_run(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies
     check_ctx(ctx);
     if (!circuit) fail(GKRGPU_ERR_INVALID, "null circuit");
     if (circuit->device != ctx->device) fail(GKRGPU_ERR_INVALID, "circuit was loaded on another device");
+    if (circuit->field == GKRGPU_FIELD_BN254) {
+        // one thread per copy: any count whose row tiles leave at most 1024 lane groups
+        if (n_copies < 1 || n_copies > (1u << 16)) fail(GKRGPU_ERR_INVALID, "n_copies must be in [1, 65536], got %u", n_copies);
+        for (int k = K_BN_LOAD; k < K_NUM_KERNELS; k++)
+            if (n_copies / geo_bn(*ctx, n_copies, k).tpr > 1024)
+                fail(GKRGPU_ERR_INVALID, "more than 1024 lane groups for %u copies; raise threads_per_row", n_copies);
+        return;
+    }
     if (n_copies < 4 || n_copies % 4 || n_copies > (1u << 16))
         fail(GKRGPU_ERR_INVALID, "n_copies must be a multiple of 4 in [4, 65536], got %u", n_copies);
     const uint32_t Q = n_copies / 4;
-    for (int k = 0; k < K_NUM_KERNELS; k++) {
+    for (int k = 0; k < K_BN_LOAD; k++) {
         const Geo g = ctx->geo(n_copies, k);
         if (g.tpr * (Q / g.tpr) != Q) fail(GKRGPU_ERR_INVALID, "no row tile divides %u copies", n_copies);
         if (Q / g.tpr > 1024) fail(GKRGPU_ERR_INVALID, "more than 1024 lane groups; raise threads_per_row");
     }
 }
 
+// Commitment (the input rows) + grinding + per layer R x (2n rounds x 3 rows + vx + vy).
 uint64_t proof_bytes(const gkrgpu_circuit* c, uint32_t N, int R) {
+    const uint64_t eb = elem_bytes(c->field);
     uint64_t rows = 0;
     for (const auto& l : c->layers) rows += (uint64_t)R * (6ull * l.nin + 2);
-    return c->in_rows(0) * N * 4 + 32 + rows * N * 4;
+    return c->in_rows(0) * N * eb + 32 + rows * N * eb;
 }
 
 // ------------------------------------------------------------------ job pipeline
@@ -986,7 +1044,8 @@ void parallel_copy_and_hash(uint8_t* dst, const uint8_t* src, uint64_t n, uint8_
 }
 
 TranscriptState host_stage(gkrgpu_ctx& c, gkrgpu_job& j, cudaStream_t s) {
-    const uint64_t in_bytes = j.circuit->in_rows(0) * (uint64_t)j.N * 4;
+    const bool bn = j.circuit->field == GKRGPU_FIELD_BN254;
+    const uint64_t in_bytes = j.circuit->in_rows(0) * (uint64_t)j.N * elem_bytes(j.circuit->field);
     uint8_t d[32];
     if (j.h_input) {
         parallel_copy_and_hash(j.proof_out, reinterpret_cast<const uint8_t*>(j.h_input), in_bytes, d);
@@ -998,7 +1057,10 @@ TranscriptState host_stage(gkrgpu_ctx& c, gkrgpu_job& j, cudaStream_t s) {
     }
     Transcript t(j.proof_out, ~0ull);
     t.appended_prehashed(in_bytes, d);
-    grind(t, j.grinding);
+    if (bn)
+        grind_bn254(t, j.grinding);
+    else
+        grind(t, j.grinding);
     return t.state();
 }
 
@@ -1052,17 +1114,27 @@ void gpu_worker(gkrgpu_ctx* c, Lane* lane) {
         }
         int rc = GKRGPU_OK;
         std::string err;
-        const uint64_t need = workspace_bytes(*j->circuit, j->N, j->R, j->d_input == nullptr, true);
+        const bool bn = j->circuit->field == GKRGPU_FIELD_BN254;
+        const uint64_t need = bn ? workspace_bytes_bn(*j->circuit, j->N, true)
+                                 : workspace_bytes(*j->circuit, j->N, j->R, j->d_input == nullptr, true);
         c->acquire_hbm(need);
         try {
-            Prover p(*c, *lane, *j->circuit, j->N, j->R);
-            p.device_front(j->h_input, j->d_input);
-            {
+            auto wait_host = [&] {
                 std::unique_lock<std::mutex> lk(j->m);
                 j->cv.wait(lk, [&] { return j->host_done; });
+                if (j->host_rc) throw Error(j->host_rc, j->host_err);
+            };
+            if (bn) {
+                BnProver p(*c, *lane, *j->circuit, j->N);
+                p.device_front(j->h_input, j->d_input);
+                wait_host();
+                p.device_back(j->ts, j->proof_out, j->claimed_v);
+            } else {
+                Prover p(*c, *lane, *j->circuit, j->N, j->R);
+                p.device_front(j->h_input, j->d_input);
+                wait_host();
+                p.device_back(j->ts, j->proof_out, j->claimed_v);
             }
-            if (j->host_rc) throw Error(j->host_rc, j->host_err);
-            p.device_back(j->ts, j->proof_out, j->claimed_v);
             if (j->marker >= 0) {
                 std::lock_guard<std::mutex> lk(c->stats_m);
                 if (!c->markers[j->marker]) ck(cudaEventCreate(&c->markers[j->marker]), "cudaEventCreate");
@@ -1100,7 +1172,7 @@ gkrgpu_job* submit(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_co
                    uint32_t* claimed_v, int marker, uint64_t* need_out) {
     check_run(ctx, circuit, n_copies);
     if (grinding_bits < 0 || grinding_bits > 30) fail(GKRGPU_ERR_INVALID, "grinding_bits must be in [0, 30]");
-    const int R = reps_for(grinding_bits);
+    const int R = reps_for_field(circuit->field, grinding_bits);
     if (R < 1 || R > 3) fail(GKRGPU_ERR_INVALID, "grinding_bits %d gives %d repetitions (1..3 supported)", grinding_bits, R);
     if (!(h_input || d_input) || !proof_out || !claimed_v) fail(GKRGPU_ERR_INVALID, "null buffer");
     if (d_input && ((uintptr_t)d_input & 15)) fail(GKRGPU_ERR_INVALID, "device input must be 16-byte aligned");
@@ -1192,6 +1264,12 @@ const char* gkrgpu_version(void) {
 
 int gkrgpu_num_repetitions(int grinding_bits) { return reps_for(grinding_bits); }
 
+int gkrgpu_num_repetitions_field(int field, int grinding_bits) {
+    return field_supported(field) ? reps_for_field(field, grinding_bits) : -GKRGPU_ERR_INVALID;
+}
+
+uint32_t gkrgpu_field_bytes(int field) { return field_supported(field) ? elem_bytes(field) : 0u; }
+
 int gkrgpu_create(int device, gkrgpu_ctx** out) {
     return guarded([&] {
         if (!out) fail(GKRGPU_ERR_INVALID, "null output");
@@ -1265,21 +1343,30 @@ int gkrgpu_memory_stats(gkrgpu_ctx* ctx, uint64_t* in_use, uint64_t* peak, uint6
 
 uint64_t gkrgpu_workspace_bytes(const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits, int input_on_device) {
     if (!circuit) return 0;
+    if (circuit->field == GKRGPU_FIELD_BN254) return workspace_bytes_bn(*circuit, n_copies, true);
     return workspace_bytes(*circuit, n_copies, reps_for(grinding_bits), input_on_device == 0, true);
 }
 
 int gkrgpu_circuit_load(gkrgpu_ctx* ctx, const gkrgpu_layer_desc* layers, int n_layers, gkrgpu_circuit** out) {
+    return gkrgpu_circuit_load_field(ctx, layers, n_layers, GKRGPU_FIELD_M31, out);
+}
+
+int gkrgpu_circuit_field(const gkrgpu_circuit* circuit) { return circuit ? circuit->field : -GKRGPU_ERR_INVALID; }
+
+int gkrgpu_circuit_load_field(gkrgpu_ctx* ctx, const gkrgpu_layer_desc* layers, int n_layers, int field,
+                              gkrgpu_circuit** out) {
     return guarded([&] {
         check_ctx(ctx);
         if (!out) fail(GKRGPU_ERR_INVALID, "null output");
         *out = nullptr;
-        validate_layers(layers, n_layers);
+        validate_layers(layers, n_layers, field);
         DeviceGuard dg(ctx->device);
         gkrgpu_circuit* c = new gkrgpu_circuit();
         c->device = ctx->device;
+        c->field = field;
         try {
             for (int l = 0; l < n_layers; l++) {
-                c->layers.push_back(upload_layer(layers[l]));
+                c->layers.push_back(upload_layer(layers[l], field));
                 c->max_in_vars = std::max(c->max_in_vars, layers[l].nb_input_vars);
                 c->max_out_vars = std::max(c->max_out_vars, layers[l].nb_output_vars);
                 c->max_mul = std::max<uint64_t>(c->max_mul, layers[l].n_mul);
@@ -1317,8 +1404,13 @@ int gkrgpu_evaluate(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_c
         check_run(ctx, circuit, n_copies);
         if (!input || !out) fail(GKRGPU_ERR_INVALID, "null buffer");
         on_idle_lane(ctx, [&](Lane& lane) {
-            Prover p(*ctx, lane, *circuit, n_copies, 1);
-            p.evaluate_only(input, out, all_layers != 0);
+            if (circuit->field == GKRGPU_FIELD_BN254) {
+                BnProver p(*ctx, lane, *circuit, n_copies);
+                p.evaluate_only(input, out, all_layers != 0);
+            } else {
+                Prover p(*ctx, lane, *circuit, n_copies, 1);
+                p.evaluate_only(input, out, all_layers != 0);
+            }
         });
     });
 }
@@ -1557,10 +1649,13 @@ int gkrgpu_autotune(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_c
         check_run(ctx, circuit, n_copies);
         if (!input) fail(GKRGPU_ERR_INVALID, "null input");
         ctx->drain();
-        const int R = reps_for(grinding_bits);
+        const bool bn = circuit->field == GKRGPU_FIELD_BN254;
+        const int R = reps_for_field(circuit->field, grinding_bits);
         if (R < 1 || R > 3) fail(GKRGPU_ERR_INVALID, "unsupported grinding_bits");
         std::vector<uint8_t> proof(proof_bytes(circuit, n_copies, R));
-        std::vector<uint32_t> cv((size_t)R * n_copies);
+        std::vector<uint32_t> cv((size_t)R * n_copies * elem_bytes(circuit->field) / 4);
+        // effective threads per row slice of kind k for this circuit's field
+        auto tile_tpr = [&](int k) { return k >= K_BN_LOAD ? geo_bn(*ctx, n_copies, k).tpr : ctx->geo(n_copies, k).tpr; };
         const bool saved_timing = ctx->timing;
         const auto saved_tiles = std::vector<gkrgpu_ctx::Tile>(std::begin(ctx->tiles), std::end(ctx->tiles));
         ctx->timing = true;
@@ -1579,7 +1674,9 @@ int gkrgpu_autotune(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_c
             snapshot(b);
             for (int k = 0; k < K_NUM_KERNELS; k++) ms[k] = b[k] - a[k];
         };
-        const int kinds[] = {K_EVALUATE, K_HG_ROUND0, K_ROUND_LANE, K_ROUND_SCALAR, K_WSUM};
+        const std::vector<int> kinds =
+            bn ? std::vector<int>{K_BN_EVALUATE, K_BN_HG_ROUND0, K_BN_ROUND_LANE, K_BN_ROUND_SCALAR, K_BN_WSUM}
+               : std::vector<int>{K_EVALUATE, K_HG_ROUND0, K_ROUND_LANE, K_ROUND_SCALAR, K_WSUM};
         try {
             double ms[K_NUM_KERNELS];
             run(ms);  // warm-up: pool growth, first-launch costs
@@ -1594,7 +1691,7 @@ int gkrgpu_autotune(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_c
             std::vector<uint32_t> seen;
             for (uint32_t t : {8u, 16u, 32u, 64u, 128u}) {
                 for (auto& tl : ctx->tiles) tl = gkrgpu_ctx::Tile{t, 0};
-                const uint32_t eff = ctx->geo(n_copies, K_ROUND_LANE).tpr;
+                const uint32_t eff = tile_tpr(bn ? K_BN_ROUND_LANE : K_ROUND_LANE);
                 if (std::find(seen.begin(), seen.end(), eff) != seen.end()) continue;
                 seen.push_back(eff);
                 run(ms);
@@ -1617,7 +1714,7 @@ int gkrgpu_autotune(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_c
             for (int k = 0; k < K_NUM_KERNELS; k++) ctx->tiles[k] = gkrgpu_ctx::Tile{best_tpr[k], best_ctas[k]};
             if (out)
                 for (int k = 0; k < K_NUM_KERNELS && k < cap; k++) {
-                    out[k].threads_per_row = ctx->geo(n_copies, k).tpr;
+                    out[k].threads_per_row = tile_tpr(k);
                     out[k].ctas = ctx->cta_budget(k);
                     out[k].ms = best_ms[k] < 1e300 ? best_ms[k] : 0.0;
                 }

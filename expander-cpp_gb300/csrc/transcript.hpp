@@ -9,6 +9,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include "fr_host.hpp"
 #include "m31.cuh"
 #include "sha256.hpp"
 
@@ -70,6 +71,15 @@ class Transcript {
     }
 
     uint32_t challenge() {
+        uint32_t x;
+        memcpy(&x, next_digest(), 4);
+        return m31::from_u32(x);
+    }
+    // BN254 challenge_f: the whole digest, read little-endian and reduced mod r.
+    frh::Fr challenge_bn254() { return frh::from_bytes(next_digest()); }
+
+    // The digest behind the next challenge (_hash_to_digest, transcript.hpp:91-103).
+    const uint8_t* next_digest() {
         if (has_pre_ && s_.hash_start == pre_from_ && s_.len == pre_to_) {
             memcpy(s_.digest, pre_, 32);
             s_.hash_start = s_.len;
@@ -82,9 +92,7 @@ class Transcript {
             sha256(s_.digest, 32, d);
             memcpy(s_.digest, d, 32);
         }
-        uint32_t x;
-        memcpy(&x, s_.digest, 4);
-        return m31::from_u32(x);
+        return s_.digest;
     }
 
    private:
@@ -105,6 +113,18 @@ inline void grind(Transcript& t, int grinding_bits) {
         const uint32_t c = t.challenge();
         memcpy(h + 4 * i, &c, 4);
     }
+    for (long i = 0; i < (1L << grinding_bits); i++) {
+        uint8_t d[32];
+        sha256(h, 32, d);
+        memcpy(h, d, 32);
+    }
+    t.append(h, 32);
+}
+
+// The same for BN254: 256/254 = 1 challenge, written as its 32 canonical bytes.
+inline void grind_bn254(Transcript& t, int grinding_bits) {
+    uint8_t h[32];
+    frh::to_bytes(t.challenge_bn254(), h);
     for (long i = 0; i < (1L << grinding_bits); i++) {
         uint8_t d[32];
         sha256(h, 32, d);

@@ -11,6 +11,9 @@ LIB_PATH = os.path.join(PKG, "libgkrgpu.so")
 
 OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_CAPACITY, ERR_TIMEOUT, ERR_STATE = range(7)
 
+# Field_type numbering of include/configuration/config.hpp:12-16 (GKRGPU_FIELD_*).
+FIELDS = {"M31": 0, "BabyBear": 1, "BN254": 2}
+
 
 class GkrGpuError(RuntimeError):
     def __init__(self, code, msg):
@@ -47,9 +50,13 @@ SIGNATURES = [
     ("gkrgpu_last_error", ctypes.c_char_p, []),
     ("gkrgpu_version", ctypes.c_char_p, []),
     ("gkrgpu_num_repetitions", _I, [_I]),
+    ("gkrgpu_num_repetitions_field", _I, [_I, _I]),
+    ("gkrgpu_field_bytes", _U32, [_I]),
     ("gkrgpu_create", _I, [_I, ctypes.POINTER(_P)]),
     ("gkrgpu_destroy", None, [_P]),
     ("gkrgpu_circuit_load", _I, [_P, _P, _I, ctypes.POINTER(_P)]),
+    ("gkrgpu_circuit_load_field", _I, [_P, _P, _I, _I, ctypes.POINTER(_P)]),
+    ("gkrgpu_circuit_field", _I, [_P]),
     ("gkrgpu_circuit_free", None, [_P]),
     ("gkrgpu_proof_size", _U64, [_P, _U32, _I]),
     ("gkrgpu_value_rows", _U64, [_P, _I]),

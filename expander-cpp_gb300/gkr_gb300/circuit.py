@@ -77,8 +77,10 @@ class Circuit:
     def nb_add_gates(self) -> int:
         return sum(l.nb_add_gates for l in self.layers)
 
-    def validate(self) -> None:
-        """Raises ValueError for inconsistent widths, out-of-range ids or coefficients."""
+    def validate(self, field: str = "M31") -> None:
+        """Raises ValueError for inconsistent widths, out-of-range ids or coefficients (M31
+        coefficients must be below p; every uint32 is a canonical BN254 coefficient)."""
+        limit = 1 << 32 if field == "BN254" else P
         if not self.layers:
             raise ValueError("circuit has no layers")
         for k, l in enumerate(self.layers):
@@ -87,9 +89,9 @@ class Circuit:
             if k + 1 < len(self.layers) and l.nb_output_vars != self.layers[k + 1].nb_input_vars:
                 raise ValueError(f"layer {k}: nb_output_vars != nb_input_vars of layer {k + 1}")
             O, I = 1 << l.nb_output_vars, 1 << l.nb_input_vars
-            if l.nb_mul_gates and (l.mul[:, 0].max() >= O or l.mul[:, 1:3].max() >= I or l.mul[:, 3].max() >= P):
+            if l.nb_mul_gates and (l.mul[:, 0].max() >= O or l.mul[:, 1:3].max() >= I or l.mul[:, 3].max() >= limit):
                 raise ValueError(f"layer {k}: mul gate id or coefficient out of range")
-            if l.nb_add_gates and (l.add[:, 0].max() >= O or l.add[:, 1].max() >= I or l.add[:, 2].max() >= P):
+            if l.nb_add_gates and (l.add[:, 0].max() >= O or l.add[:, 1].max() >= I or l.add[:, 2].max() >= limit):
                 raise ValueError(f"layer {k}: add gate id or coefficient out of range")
 
     def proof_size(self, n_copies: int, reps: int = 3) -> int:

@@ -20,18 +20,39 @@ from .circuit import Circuit
 
 
 class Config:
-    """Config of the reference: 100-bit security, RAW commitment, M31, SHA-256 transcript."""
+    """Config of the reference: 100-bit security, RAW commitment, SHA-256 transcript, field
+    M31 (default) or BN254 (config.hpp:12-16,40-86)."""
 
-    def __init__(self, grinding_bits: int = 10):
+    def __init__(self, grinding_bits: int = 10, field_type: str = "M31"):
+        if field_type not in ("M31", "BN254"):
+            raise ValueError(f"unsupported field_type {field_type!r} (M31 or BN254)")
         self.security_bits = 100
         self.grinding_bits = int(grinding_bits)
-        self.field_size = 31
+        self.field_type = field_type
+        self.field_size = 254 if field_type == "BN254" else 31
         self.PC_type = "Raw"
-        self.field_type = "M31"
         self.FS_hash = "SHA256"
 
     def get_num_repetitions(self) -> int:
-        return _lib.load().gkrgpu_num_repetitions(self.grinding_bits)
+        return _lib.load().gkrgpu_num_repetitions_field(_lib.FIELDS[self.field_type], self.grinding_bits)
+
+
+def _table(field: str, values):
+    """A value table in the C layout: M31 (rows, N) uint32; BN254 (rows, N, 4) uint64 limbs
+    (little-endian, i.e. the 32 canonical bytes of each element)."""
+    if field == "BN254":
+        a = np.ascontiguousarray(values, dtype=np.uint64)
+        if a.ndim != 3 or a.shape[2] != 4:
+            raise ValueError("a BN254 table is a (rows, N, 4) uint64 array")
+        return a
+    a = np.ascontiguousarray(values, dtype=np.uint32)
+    if a.ndim != 2:
+        raise ValueError("an M31 table is a (rows, N) uint32 array")
+    return a
+
+
+def _empty(field: str, rows: int, n: int):
+    return np.empty((rows, n, 4), np.uint64) if field == "BN254" else np.empty((rows, n), np.uint32)
 
 
 class Proof:
@@ -60,12 +81,13 @@ class Proof:
 
 
 class DeviceCircuit:
-    """A circuit's wiring resident on the device (gkrgpu_circuit_load)."""
+    """A circuit's wiring resident on the device (gkrgpu_circuit_load_field)."""
 
-    def __init__(self, ctx: "Context", circuit: Circuit):
+    def __init__(self, ctx: "Context", circuit: Circuit, field: str = "M31"):
         lib = _lib.load()
-        circuit.validate()
+        circuit.validate(field)
         self.ctx = ctx
+        self.field = field
         self.n_layers = len(circuit.layers)
         self.log_input_size = circuit.log_input_size
         self.nb_output_vars = circuit.layers[-1].nb_output_vars
@@ -78,11 +100,14 @@ class DeviceCircuit:
             descs[k] = _lib.LayerDesc(l.nb_output_vars, l.nb_input_vars, m.shape[0], a.shape[0],
                                       m.ctypes.data if m.size else None, a.ctypes.data if a.size else None)
         h = ctypes.c_void_p()
-        _lib.check(lib.gkrgpu_circuit_load(ctx.handle, descs, self.n_layers, ctypes.byref(h)))
+        _lib.check(lib.gkrgpu_circuit_load_field(ctx.handle, descs, self.n_layers, _lib.FIELDS[field], ctypes.byref(h)))
         self.handle = h
 
     def proof_size(self, n_copies, grinding_bits=10):
         return _lib.load().gkrgpu_proof_size(self.handle, n_copies, grinding_bits)
+
+    def num_repetitions(self, grinding_bits=10):
+        return _lib.load().gkrgpu_num_repetitions_field(_lib.FIELDS[self.field], grinding_bits)
 
     def free(self):
         if getattr(self, "handle", None):
@@ -117,30 +142,29 @@ class Context:
         except Exception:
             pass
 
-    def load(self, circuit: Circuit) -> DeviceCircuit:
-        return DeviceCircuit(self, circuit)
+    def load(self, circuit: Circuit, field: str = "M31") -> DeviceCircuit:
+        return DeviceCircuit(self, circuit, field)
 
     def evaluate(self, dc: DeviceCircuit, witness, all_layers=False):
         """Circuit::evaluate on the device; returns the output rows, or with all_layers every
-        layer's input rows followed by the output rows, as one (rows, N) array."""
+        layer's input rows followed by the output rows, as one (rows, N) table."""
         lib = _lib.load()
-        w = np.ascontiguousarray(witness, dtype=np.uint32)
+        w = _table(dc.field, witness)
         rows = lib.gkrgpu_value_rows(dc.handle, int(all_layers))
-        out = np.empty((rows, w.shape[1]), np.uint32)
+        out = _empty(dc.field, rows, w.shape[1])
         _lib.check(lib.gkrgpu_evaluate(self.handle, dc.handle, w.shape[1], w.ctypes.data, out.ctypes.data,
                                        int(all_layers)))
         return out
 
     def prove(self, dc: DeviceCircuit, witness, grinding_bits=10, out=None):
-        """Prover::prove; returns (claimed_v (R, N) uint32, proof bytes).  `out` may be a
+        """Prover::prove; returns (claimed_v (R, N) table, proof bytes).  `out` may be a
         preallocated uint8 buffer of at least proof_size bytes (e.g. pinned host memory)."""
         lib = _lib.load()
-        w = np.ascontiguousarray(witness, dtype=np.uint32)
+        w = _table(dc.field, witness)
         N = w.shape[1]
         cap = dc.proof_size(N, grinding_bits)
         buf = np.empty(cap, np.uint8) if out is None else out
-        R = lib.gkrgpu_num_repetitions(grinding_bits)
-        cv = np.empty((R, N), np.uint32)
+        cv = _empty(dc.field, dc.num_repetitions(grinding_bits), N)
         plen = ctypes.c_uint64()
         _lib.check(lib.gkrgpu_prove(self.handle, dc.handle, N, grinding_bits, w.ctypes.data, buf.ctypes.data,
                                     buf.nbytes, ctypes.byref(plen), cv.ctypes.data))
@@ -149,8 +173,7 @@ class Context:
     def prove_device(self, dc: DeviceCircuit, d_input: int, n_copies: int, out_buf, grinding_bits=10):
         """Prover::prove with the input already in device memory at address d_input."""
         lib = _lib.load()
-        R = lib.gkrgpu_num_repetitions(grinding_bits)
-        cv = np.empty((R, n_copies), np.uint32)
+        cv = _empty(dc.field, dc.num_repetitions(grinding_bits), n_copies)
         plen = ctypes.c_uint64()
         _lib.check(lib.gkrgpu_prove_device(self.handle, dc.handle, n_copies, grinding_bits, ctypes.c_void_p(d_input),
                                            out_buf.ctypes.data, out_buf.nbytes, ctypes.byref(plen), cv.ctypes.data))
@@ -165,7 +188,7 @@ class Context:
         if d_input is not None:
             src, on_dev, n, keep = ctypes.c_void_p(d_input), 1, claimed_buf.shape[1], None
         else:
-            keep = np.ascontiguousarray(witness, dtype=np.uint32)
+            keep = _table(dc.field, witness)
             src, on_dev, n = keep.ctypes.data, 0, keep.shape[1]
         _lib.check(lib.gkrgpu_prove_submit(self.handle, dc.handle, n, grinding_bits, src, on_dev,
                                            proof_buf.ctypes.data, proof_buf.nbytes, claimed_buf.ctypes.data, marker,
@@ -212,7 +235,7 @@ class Context:
         if d_input is not None:
             src, on_dev, n, keep = ctypes.c_void_p(d_input), 1, n_copies, None
         else:
-            keep = np.ascontiguousarray(witness, dtype=np.uint32)
+            keep = _table(dc.field, witness)
             src, on_dev, n = keep.ctypes.data, 0, keep.shape[1]
         _lib.check(lib.gkrgpu_autotune(self.handle, dc.handle, n, grinding_bits, src, on_dev, arr, 32))
         names = list(self.kernel_stats().keys())
@@ -310,7 +333,7 @@ class Prover:
     def prepare_mem(self, circuit: Circuit):
         """Uploads the circuit's wiring (the reference allocates its scratch pads here)."""
         if self._circuit is not circuit:
-            self._dc = self.ctx.load(circuit)
+            self._dc = self.ctx.load(circuit, self.config.field_type)
             self._circuit = circuit
 
     def prove(self, circuit: Circuit, witness=None):

@@ -10,6 +10,10 @@
  * values, row-major (row i, copy k at i*N + k), each canonical in [0, 2^31 - 1).  One row
  * is the byte image of the reference's vector field element (VectorizedM31::to_bytes,
  * include/field/M31.hpp:420-426) for N copies.
+ *
+ * BN254 circuits (gkrgpu_circuit_load_field with GKRGPU_FIELD_BN254): an element is 8
+ * uint32 words, the canonical integer in [0, r) as 32 little-endian bytes, so a row is
+ * 8*N words and every uint32_t* table argument below holds 8 words per value.  R = 1.
  */
 #ifndef GKRGPU_H
 #define GKRGPU_H
@@ -28,6 +32,12 @@ extern "C" {
 #define GKRGPU_ERR_CAPACITY 4  /* caller buffer too small (required size still reported) */
 #define GKRGPU_ERR_TIMEOUT 5   /* a bounded wait expired */
 #define GKRGPU_ERR_STATE 6     /* object used in the wrong state */
+
+/* Field_type, include/configuration/config.hpp:12-16 (same numbering).  BabyBear is
+ * declared there without a prover and is rejected here too. */
+#define GKRGPU_FIELD_M31 0
+#define GKRGPU_FIELD_BABYBEAR 1
+#define GKRGPU_FIELD_BN254 2
 
 typedef struct gkrgpu_ctx gkrgpu_ctx;
 typedef struct gkrgpu_circuit gkrgpu_circuit;
@@ -63,6 +73,13 @@ const char* gkrgpu_version(void);
  * include/configuration/config.hpp:61-65 (3 for the default grinding_bits = 10). */
 int gkrgpu_num_repetitions(int grinding_bits);
 
+/* The same for any supported field: ceil((100 - grinding_bits) / field_size), field_size 31
+ * (M31) or 254 (BN254), config.hpp:40-65.  Negative for an unsupported field. */
+int gkrgpu_num_repetitions_field(int field, int grinding_bits);
+
+/* Bytes of one element of `field` in every table and in the proof (4 or 32; 0 if unsupported). */
+uint32_t gkrgpu_field_bytes(int field);
+
 /* A context owns one CUDA device, a stream and a reusable device workspace.
  * Replaces the reference's per-prover scratch (GKRScratchPad,
  * include/LinearGKR/scratch_pad.hpp:8-65; Prover::prepare_mem, LinearGKR.hpp:49-56). */
@@ -74,6 +91,16 @@ void gkrgpu_destroy(gkrgpu_ctx* ctx);
  * (include/circuit/circuit.hpp:118-251).  Ids and coefficients are checked. */
 int gkrgpu_circuit_load(gkrgpu_ctx* ctx, const gkrgpu_layer_desc* layers, int n_layers, gkrgpu_circuit** out);
 void gkrgpu_circuit_free(gkrgpu_circuit* circuit);
+
+/* As gkrgpu_circuit_load for the field Config::field_type names (GKRGPU_FIELD_*).  Every
+ * later call on the circuit works in that field: BN254 tables hold 8 words per value,
+ * coefficients are any uint32 (canonical in BN254), R = 1 and n_copies may be any count
+ * in [1, 65536].  gkrgpu_circuit_load is this call with GKRGPU_FIELD_M31. */
+int gkrgpu_circuit_load_field(gkrgpu_ctx* ctx, const gkrgpu_layer_desc* layers, int n_layers, int field,
+                              gkrgpu_circuit** out);
+
+/* Field of a loaded circuit (GKRGPU_FIELD_*), negative for a null circuit. */
+int gkrgpu_circuit_field(const gkrgpu_circuit* circuit);
 
 /* Proof bytes of Prover::prove for this circuit: RAW commitment (2^nb_input_vars(0) rows
  * of 4N bytes) + 32 grinding bytes + per layer R*(6*nb_input_vars + 2) rows of 4N bytes. */

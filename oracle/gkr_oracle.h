@@ -60,6 +60,21 @@ void oracle_sha256(const uint8_t* in, uint64_t len, uint8_t out[32]);
 double oracle_bench(const oracle_layer* layers, int nlayers, uint32_t n_copies, const uint32_t* input,
                     int grinding_bits, int n_threads, int proofs_per_thread);
 
+/* BN254 (gkr_oracle_bn254.c): the same calls with one repetition.  Tables hold 4 uint64
+ * limbs per element (its 32 canonical little-endian bytes); coefficients are any uint32;
+ * claimed_v is N elements.  prove/evaluate return -1 on an input element >= r. */
+int oracle_bn254_num_repetitions(int grinding_bits);
+uint64_t oracle_bn254_proof_size(const oracle_layer* layers, int nlayers, uint32_t n_copies);
+int oracle_bn254_evaluate(const oracle_layer* layers, int nlayers, uint32_t n_copies, const uint64_t* input,
+                          uint64_t* out);
+int oracle_bn254_prove(const oracle_layer* layers, int nlayers, uint32_t n_copies, const uint64_t* input,
+                       int grinding_bits, uint8_t* proof_out, uint64_t proof_cap, uint64_t* proof_len,
+                       uint64_t* claimed_v);
+int oracle_bn254_verify(const oracle_layer* layers, int nlayers, uint32_t n_copies, const uint64_t* input,
+                        int grinding_bits, const uint8_t* proof, uint64_t proof_len, const uint64_t* claimed_v);
+double oracle_bn254_bench(const oracle_layer* layers, int nlayers, uint32_t n_copies, const uint64_t* input,
+                          int grinding_bits, int n_threads, int proofs_per_thread);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,6 +122,72 @@ class Oracle:
         return t
 
 
+class OracleBn254:
+    """The C restatement over BN254 (oracle/gkr_oracle_bn254.c).  Tables are (rows, N, 4)
+    uint64 limb arrays; claimed_v is (1, N, 4)."""
+
+    def __init__(self, path=None):
+        path = path or _build.build_oracle()
+        self.lib = ctypes.CDLL(path)
+        L = self.lib
+        P, I, U32, U64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64
+        L.oracle_bn254_prove.argtypes = [P, I, U32, P, I, P, U64, ctypes.POINTER(U64), P]
+        L.oracle_bn254_verify.argtypes = [P, I, U32, P, I, P, U64, P]
+        L.oracle_bn254_evaluate.argtypes = [P, I, U32, P, P]
+        L.oracle_bn254_proof_size.argtypes = [P, I, U32]
+        L.oracle_bn254_proof_size.restype = U64
+        L.oracle_bn254_bench.argtypes = [P, I, U32, P, I, I, I]
+        L.oracle_bn254_bench.restype = ctypes.c_double
+
+    def proof_size(self, circuit, n_copies):
+        arr, keep = _layers(circuit)
+        return self.lib.oracle_bn254_proof_size(arr, len(circuit.layers), n_copies)
+
+    def prove(self, circuit, witness, grinding_bits=10):
+        w = np.ascontiguousarray(witness, dtype=np.uint64)
+        N = w.shape[1]
+        cap = self.proof_size(circuit, N)
+        proof = np.empty(cap, np.uint8)
+        cv = np.empty((1, N, 4), np.uint64)
+        plen = ctypes.c_uint64()
+        arr, keep = _layers(circuit)
+        rc = self.lib.oracle_bn254_prove(arr, len(circuit.layers), N, w.ctypes.data, grinding_bits, proof.ctypes.data,
+                                         cap, ctypes.byref(plen), cv.ctypes.data)
+        if rc != 0:
+            raise ValueError(f"oracle_bn254_prove failed rc={rc}")
+        return cv, proof[:plen.value].tobytes()
+
+    def verify(self, circuit, witness, claimed_v, proof, grinding_bits=10):
+        w = np.ascontiguousarray(witness, dtype=np.uint64)
+        cv = np.ascontiguousarray(claimed_v, dtype=np.uint64)
+        pb = np.frombuffer(bytes(proof), np.uint8)
+        arr, keep = _layers(circuit)
+        rc = self.lib.oracle_bn254_verify(arr, len(circuit.layers), w.shape[1], w.ctypes.data, grinding_bits,
+                                          pb.ctypes.data, len(pb), cv.ctypes.data)
+        if rc < 0:
+            raise ValueError("oracle_bn254_verify: bad input")
+        return rc == 1
+
+    def evaluate(self, circuit, witness):
+        w = np.ascontiguousarray(witness, dtype=np.uint64)
+        N = w.shape[1]
+        sizes = [1 << l.nb_input_vars for l in circuit.layers] + [1 << circuit.layers[-1].nb_output_vars]
+        out = np.empty((sum(sizes), N, 4), np.uint64)
+        arr, keep = _layers(circuit)
+        if self.lib.oracle_bn254_evaluate(arr, len(circuit.layers), N, w.ctypes.data, out.ctypes.data) != 0:
+            raise ValueError("oracle_bn254_evaluate: bad input")
+        return np.split(out, np.cumsum(sizes)[:-1])
+
+    def bench(self, circuit, witness, n_threads, proofs_per_thread, grinding_bits=10):
+        w = np.ascontiguousarray(witness, dtype=np.uint64)
+        arr, keep = _layers(circuit)
+        t = self.lib.oracle_bn254_bench(arr, len(circuit.layers), w.shape[1], w.ctypes.data, grinding_bits,
+                                        n_threads, proofs_per_thread)
+        if t < 0:
+            raise RuntimeError("oracle_bn254_bench failed")
+        return t
+
+
 class Reference:
     """The compiled, unmodified reference prover/verifier (x86-64 build only)."""
 

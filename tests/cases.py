@@ -70,3 +70,44 @@ def build(name):
     circ, n, grind = CASES[name]()
     seed = sum(ord(c) for c in name) * 7919
     return circ, gc.random_witness(seed, circ.log_input_size, n), grind
+
+
+# ---------------------------------------------------------------- BN254 (Config::field_type = BN254)
+def _full_range_coefs(circ, seed):
+    # coefficients anywhere in [0, 2^32): canonical BN254 elements, most of them >= 2^31 - 1
+    st = gc.Stream(seed)
+    for l in circ.layers:
+        if l.nb_mul_gates:
+            l.mul[:, 3] = (st.u64(l.nb_mul_gates) >> np.uint64(32)).astype(np.uint32)
+        if l.nb_add_gates:
+            l.add[:, 2] = (st.u64(l.nb_add_gates) >> np.uint64(32)).astype(np.uint32)
+    return circ
+
+
+BN_CASES = {
+    "bn_gkr_test_shape_n8": lambda: (_gkr_test_shape(), 8, 10),
+    "bn_mixed_widths_n16": lambda: (gc.random_circuit(5, [3, 2, 4, 1, 2]), 16, 10),
+    "bn_width_one_n4": lambda: (gc.random_circuit(6, [1, 1, 1, 1]), 4, 10),
+    "bn_output_scalar_n16": lambda: (gc.random_circuit(7, [3, 2, 0]), 16, 10),
+    "bn_full_coefs_n8": lambda: (_full_range_coefs(gc.random_circuit(21, [5, 4, 5]), 21), 8, 10),
+    "bn_all_to_one_n4": lambda: (_all_to_one(4), 4, 10),
+    "bn_no_gates_rows_n16": lambda: (_no_gates_layer(), 16, 10),
+    "bn_lanes64": lambda: (gc.random_circuit(22, [6, 5, 6]), 64, 10),
+    "bn_edge_values_n8": lambda: (gc.random_circuit(24, [4, 5, 4]), 8, 10),
+    "bn_grind0_n8": lambda: (gc.random_circuit(23, [4, 4, 4]), 8, 0),
+    "bn_grind12_n16": lambda: (gc.random_circuit(25, [4, 4, 4]), 16, 12),
+}
+
+
+def build_bn(name):
+    """(circuit, (rows, N, 4) uint64 witness, grinding_bits) of a BN254 case."""
+    circ, n, grind = BN_CASES[name]()
+    seed = sum(ord(c) for c in name) * 7919
+    w = gc.random_witness_bn254(seed, circ.log_input_size, n)
+    if name == "bn_edge_values_n8":
+        r_minus_1 = [(gc.BN254_R - 1) >> (64 * k) & (2**64 - 1) for k in range(4)]
+        w[0, :, :] = np.array(r_minus_1, np.uint64)  # r - 1 everywhere in row 0
+        w[1, :, :] = 0  # zero row
+        w[2, ::2, :] = np.array([1, 0, 0, 0], np.uint64)
+        w[3, 1::2, :] = np.array(r_minus_1, np.uint64)
+    return circ, w, grind

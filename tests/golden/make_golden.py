@@ -21,7 +21,7 @@ import numpy as np  # noqa: E402
 
 import cases  # noqa: E402
 from oracle import build as obuild  # noqa: E402
-from oracle.oracle import Reference  # noqa: E402
+from oracle.oracle import Reference, ReferenceBn254  # noqa: E402
 
 
 def digest(b):
@@ -48,6 +48,25 @@ def main():
             "values_sha256": digest(np.concatenate(ev).tobytes()),
         }
         print(name, len(proof), out["cases"][name]["proof_sha256"][:16])
+    # BN254: the reference templates over oracle/bn254.h's field (R = 1)
+    bn = ReferenceBn254()
+    out["bn254_generator"] = "reference Prover::prove templates over BN254 via oracle/_ref (N-lane LaneVec)"
+    out["bn254_cases"] = {}
+    for name in cases.BN_CASES:
+        circ, w, grind = cases.build_bn(name)
+        cv, proof = bn.prove(circ, w, grinding_bits=grind)
+        assert bn.verify(circ, w, cv, proof, grinding_bits=grind), name
+        ev = bn.evaluate(circ, w)
+        out["bn254_cases"][name] = {
+            "n_copies": int(w.shape[1]),
+            "grinding_bits": grind,
+            "proof_len": len(proof),
+            "proof_sha256": digest(proof),
+            "claimed_v_sha256": digest(np.ascontiguousarray(cv).tobytes()),
+            "output_sha256": digest(np.ascontiguousarray(ev[-1]).tobytes()),
+            "values_sha256": digest(np.concatenate(ev).tobytes()),
+        }
+        print(name, len(proof), out["bn254_cases"][name]["proof_sha256"][:16])
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
 

@@ -54,3 +54,67 @@ def test_reference_templates_prove_and_verify_bn254(refbn):
         out[o] = (out[o] + inp[i0] * c) % R
     got = [gc.bn254_values(ev[1][i, 3])[0] for i in range(len(out))]
     assert got == out
+
+
+# ---------------------------------------------------------------- the C restatement over BN254
+import hashlib  # noqa: E402
+import json  # noqa: E402
+import os  # noqa: E402
+
+import cases  # noqa: E402
+
+GOLDEN_BN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))["bn254_cases"]
+
+
+@pytest.fixture(scope="module")
+def obn():
+    from oracle.oracle import OracleBn254
+    return OracleBn254()
+
+
+def _sha(b):
+    return hashlib.sha256(bytes(b)).hexdigest()
+
+
+@pytest.mark.parametrize("name", sorted(GOLDEN_BN))
+def test_bn254_oracle_matches_reference_golden(obn, name):
+    g = GOLDEN_BN[name]
+    circ, w, grind = cases.build_bn(name)
+    cv, proof = obn.prove(circ, w, grinding_bits=grind)
+    assert len(proof) == g["proof_len"] == obn.proof_size(circ, w.shape[1])
+    assert _sha(proof) == g["proof_sha256"]
+    assert _sha(cv.tobytes()) == g["claimed_v_sha256"]
+    assert _sha(np.concatenate(obn.evaluate(circ, w)).tobytes()) == g["values_sha256"]
+    assert obn.verify(circ, w, cv, proof, grinding_bits=grind)
+
+
+def test_bn254_oracle_rejects_tampering(obn):
+    circ, w, grind = cases.build_bn("bn_mixed_widths_n16")
+    cv, proof = obn.prove(circ, w, grinding_bits=grind)
+    n0 = (1 << circ.log_input_size) * 16 * 32 + 32
+    for pos in (n0 + 5, len(proof) // 2, len(proof) - 1):
+        bad = bytearray(proof)
+        bad[pos] ^= 0x10
+        assert not obn.verify(circ, w, cv, bytes(bad), grinding_bits=grind), pos
+    cv2 = cv.copy()
+    cv2[0, 3, 0] ^= 1
+    assert not obn.verify(circ, w, cv2, proof, grinding_bits=grind)
+    assert not obn.verify(circ, w, cv, proof[:-32], grinding_bits=grind)
+
+
+def test_bn254_oracle_rejects_non_canonical_input(obn):
+    circ, w, grind = cases.build_bn("bn_width_one_n4")
+    bad = w.copy()
+    bad[1, 2, :] = np.array([R >> (64 * k) & (2**64 - 1) for k in range(4)], np.uint64)
+    with pytest.raises(ValueError):
+        obn.prove(circ, bad, grinding_bits=grind)
+
+
+@pytest.mark.parametrize("seed,widths,n", [(301, [6, 7, 5, 6], 16), (302, [8, 6, 8], 4), (303, [5, 5, 5, 5], 64)])
+def test_bn254_oracle_matches_reference_random(obn, refbn, seed, widths, n):
+    circ = gc.random_circuit(seed, widths, p_mul=0.6, p_local=0.7, window=32)
+    w = gc.random_witness_bn254(seed, circ.log_input_size, n)
+    cv, proof = obn.prove(circ, w)
+    rcv, rproof = refbn.prove(circ, w)
+    assert proof == rproof
+    assert np.array_equal(cv, rcv)
