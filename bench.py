@@ -57,10 +57,11 @@ def parse():
     ap.add_argument("--depth", type=int, default=3, help="proofs in flight (host hashing overlaps device work)")
     ap.add_argument("--tile", default="", help="threads_per_row,block,ctas for every kernel (default: autotuned)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default row tiles")
-    ap.add_argument("--workload", choices=["plain", "mixed", "serve"], default="plain",
+    ap.add_argument("--workload", choices=["plain", "mixed", "serve", "bn254"], default="plain",
                     help="plain: the large single-circuit proof; mixed: many independent proofs of mixed depth, "
                          "width and copies, plain one-at-a-time vs continuous batching; serve: open-loop Poisson "
-                         "arrivals of mixed proofs")
+                         "arrivals of mixed proofs; bn254: 16 x 2^16 BN254 circuit at 64 copies, plain and "
+                         "64 proofs batched")
     ap.add_argument("--proofs", type=int, default=512, help="mixed/serve: number of distinct proofs")
     ap.add_argument("--lanes", type=int, default=16, help="mixed/serve: proofs whose device stages overlap")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="mixed/serve: device-memory admission budget")
@@ -551,6 +552,137 @@ def run_serve(args, D):
     print(json.dumps(line), flush=True)
 
 
+def run_bn254(args, D):
+    """BN254 workload: one 16-layer circuit of 2^16 gates (50% mul / 50% add fan-in-2,
+    uniform wiring, 64 copies) proved plainly, then 64 independent proofs of widths
+    2^12..2^16 (16 layers, 64 copies, own seed each) plain vs batched."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from gkr_gb300 import circuit as gc
+    from gkr_gb300.prover import Context, DeviceBuffer, HostBuffer
+    if D.rank != 0:
+        return
+    N, depth_l, width = 64, 16, 16
+    ctx = Context(D.local_rank)
+    circ = gc.uniform_circuit(4254, depth_l, width, p_mul=0.5)
+    dc = ctx.load(circ, "BN254")
+    rows = 1 << circ.log_input_size
+    plen = dc.proof_size(N)
+    hin = HostBuffer(rows * N * 32, np.uint64)
+    witness = hin.array.reshape(rows, N, 4)
+    witness[:] = gc.random_witness_bn254(4254, circ.log_input_size, N)
+    din = DeviceBuffer(ctx, rows * N * 32)
+    din.upload(witness)
+    pbufs = [HostBuffer(plen) for _ in range(args.depth)]
+    bufs = [(pb.array, np.empty((1, N, 4), np.uint64)) for pb in pbufs]
+    tiles = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        tiles = ctx.autotune(dc, None, n_copies=N, d_input=din.ptr)
+        tiles = {"seconds": time.perf_counter() - t0,
+                 "choice": {k: {"threads_per_row": v["threads_per_row"], "ctas": v["ctas"]}
+                            for k, v in tiles.items() if v["ms"] > 0}}
+        ctx.reset_stats()
+
+    ctx.set_timing(True)
+    clocks = ClockSampler(D.local_rank)
+    clocks.start()
+    total_ms, step_ms, lat_ms, s0, s1 = pipelined(
+        ctx, args.warmup, args.steps, bufs, lambda b, m: ctx.submit(dc, None, b[0], b[1], d_input=din.ptr, marker=m))
+    clk = clocks.stop()
+    ctx.set_timing(False)
+    stats = stats_delta(s0, s1)
+    value = args.steps / (total_ms / 1000.0)
+    e2e = None
+    if not args.no_e2e:
+        h0 = ctx.transfer_stats()
+        e2e_ms, _, e2e_lat, _, _ = pipelined(ctx, 1, args.steps, bufs,
+                                            lambda b, m: ctx.submit(dc, witness, b[0], b[1], marker=m))
+        h1 = ctx.transfer_stats()
+        n_jobs = 1 + args.steps
+        e2e = {"value": args.steps / (e2e_ms / 1000.0), "unit": UNIT,
+               "h2d_bytes_per_step": (h1[0] - h0[0]) // n_jobs, "d2h_bytes_per_step": (h1[1] - h0[1]) // n_jobs,
+               "latency_ms": {"p50": statistics.median(e2e_lat), "p99": float(np.percentile(e2e_lat, 99))}}
+    kernels = {k: {"launches_per_step": v["launches"] / args.steps, "ms_per_step": v["ms"] / args.steps,
+                   "GBps": (v["bytes"] / (v["ms"] / 1000.0) / 1e9) if v["ms"] else None}
+               for k, v in stats.items() if v["launches"]}
+    peak, peak_kind = peaks()
+    name, s = max(stats.items(), key=lambda kv: kv[1]["ms"])
+    per_b, per_ms = s["bytes"] / max(s["launches"], 1), s["ms"] / max(s["launches"], 1)
+    achieved = per_b / (per_ms / 1000.0) / 1e9 if per_ms > 0 else 0.0
+    roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                "note": "256-bit Montgomery products make these kernels integer-multiply bound; the HBM fraction "
+                        "is reported for comparison"}
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle.oracle import OracleBn254
+        threads = len(os.sched_getaffinity(0))
+        cn = 8
+        w8 = gc.random_witness_bn254(7, circ.log_input_size, cn)
+        dt = OracleBn254().bench(circ, w8, threads, 1)
+        cpu = {"value": threads / dt * cn / N, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{threads} threads x 1 proof of the same circuit at {cn} copies (oracle/gkr_oracle_bn254.c, "
+                         f"evaluate + prove), scaled by {cn}/{N} to {N}-copy proofs/s"}
+
+    # ---- batched: 64 independent proofs, widths 2^12..2^16
+    n_b = 64
+    st = gc.Stream(99)
+    ks = (12 + st.below(n_b, 5)).tolist()
+    with ThreadPoolExecutor(8) as ex:
+        circs = list(ex.map(lambda i: gc.uniform_circuit(5000 + i, depth_l, int(ks[i]), p_mul=0.5), range(n_b)))
+        wits = list(ex.map(lambda i: gc.random_witness_bn254(5000 + i, int(ks[i]), N), range(n_b)))
+    dcs = [ctx.load(c, "BN254") for c in circs]
+    pbs = [np.empty(d.proof_size(N), np.uint8) for d in dcs]
+    cbs = [np.empty((1, N, 4), np.uint64) for _ in range(n_b)]
+
+    def run_all(lanes):
+        ctx.set_concurrency(lanes=lanes, hbm_budget_bytes=int(args.budget_gb * (1 << 30)))
+        for i in range(min(lanes, n_b)):
+            ctx.wait(ctx.submit(dcs[i], wits[i], pbs[i], cbs[i]))
+        lat = []
+        t0 = time.perf_counter()
+        if lanes == 1:
+            for i in range(n_b):
+                t1 = time.perf_counter()
+                ctx.wait(ctx.submit(dcs[i], wits[i], pbs[i], cbs[i]))
+                lat.append((time.perf_counter() - t1) * 1000.0)
+        else:
+            subs = [(time.perf_counter(), ctx.submit(dcs[i], wits[i], pbs[i], cbs[i])) for i in range(n_b)]
+            for t1, j in subs:
+                ctx.wait(j)
+                lat.append((time.perf_counter() - t1) * 1000.0)
+        sec = time.perf_counter() - t0
+        import hashlib
+        return n_b / sec, lat, [hashlib.sha256(p.tobytes()).hexdigest() for p in pbs]
+
+    plain_v, plain_lat, plain_d = run_all(1)
+    batch_v, batch_lat, batch_d = run_all(args.lanes)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u256 (BN254 Montgomery, 8 x u32 limbs)", "data": "synthetic",
+            "config": {"workload": f"BN254: {depth_l} layers of 2^{width} gates, 50% mul / 50% add fan-in-2, uniform "
+                                   f"wiring, {N} copies, uniform witness in [0, r), SHA-256 transcript, RAW "
+                                   "commitment (one plain proof per step)",
+                       "n_copies": N, "layers": depth_l, "width_log2": width, "field": "BN254", "repetitions": 1,
+                       "grinding_bits": 10, "pipeline": f"{args.depth} proofs in flight"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(sum(v["launches"] for v in stats.values())), "autotune": tiles, "clocks": clk,
+            "latency_ms": {"p50": statistics.median(lat_ms), "p99": float(np.percentile(lat_ms, 99)),
+                           "device_ms_per_proof": step_ms},
+            "kernels": kernels, "proof_bytes": plen,
+            "batched": {"proofs": n_b, "widths_log2": sorted(set(int(k) for k in ks)), "layers": depth_l,
+                        "n_copies": N, "lanes": args.lanes, "proofs_per_s": batch_v,
+                        "latency_ms": {"p50": statistics.median(batch_lat),
+                                       "p99": float(np.percentile(batch_lat, 99))},
+                        "plain_proofs_per_s": plain_v,
+                        "plain_latency_ms": {"p50": statistics.median(plain_lat),
+                                             "p99": float(np.percentile(plain_lat, 99))},
+                        "batched_over_plain": batch_v / plain_v, "byte_identical_to_plain": batch_d == plain_d}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     D = Dist()
@@ -561,6 +693,8 @@ def main():
             run_mixed(args, D)
         elif args.workload == "serve":
             run_serve(args, D)
+        elif args.workload == "bn254":
+            run_bn254(args, D)
         else:
             run_ours(args, D)
     finally:

@@ -282,7 +282,9 @@ class HostBuffer:
         _lib.check(_lib.load().gkrgpu_host_alloc(nbytes, ctypes.byref(p)))
         self.ptr = p.value
         self.nbytes = nbytes
-        self.array = np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(self.ptr)).view(dtype)
+        raw = (ctypes.c_uint8 * nbytes).from_address(self.ptr)
+        raw._owner = self  # views of .array keep the pinned block alive
+        self.array = np.ctypeslib.as_array(raw).view(dtype)
 
     def free(self):
         if self.ptr:

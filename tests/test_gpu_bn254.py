@@ -151,3 +151,13 @@ def test_bn254_row_tiles_do_not_change_proofs(tile):
             assert sha(proof) == BN[name]["proof_sha256"], (tile, name)
     finally:
         ctx.close()
+
+
+def test_host_buffer_views_keep_the_pinned_block_alive(ctx):
+    import gc as pygc
+
+    from gkr_gb300.prover import HostBuffer
+    a = HostBuffer(1 << 16, np.uint64).array
+    pygc.collect()
+    a[:] = 7
+    assert int(a.sum()) == 7 * (1 << 13)
