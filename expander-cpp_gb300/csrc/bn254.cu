@@ -1,7 +1,7 @@
 // BN254 scalar-field kernels (see bn254.cuh).  Same algorithms as the M31 kernels in
 // kernels.cu, for one repetition (R = 1 for BN254, include/configuration/config.hpp:61-65),
 // with 256-bit elements: one thread per element of a row, Montgomery multiplication on
-// 8 x 32-bit limbs (CIOS, 64-bit multiply-accumulate chains).
+// 8 x 32-bit limbs (CIOS as PTX multiply-add carry chains).
 #include "bn254.cuh"
 
 namespace gkrgpu {
@@ -9,31 +9,14 @@ namespace bn {
 
 namespace {
 
-__constant__ uint32_t kR[8] = {0xf0000001u, 0x43e1f593u, 0x79b97091u, 0x2833e848u,
-                               0x8181585du, 0xb85045b6u, 0xe131a029u, 0x30644e72u};
+// r = 0x30644e72e131a029b85045b68181585d2833e84879b9709143e1f593f0000001 (little-endian
+// limbs 0xf0000001, 0x43e1f593, ... appear as immediates in the PTX below), -r^-1 mod 2^32 =
+// 0xefffffff.
 __constant__ uint32_t kOne[8] = {0x4ffffffbu, 0xac96341cu, 0x9f60cd29u, 0x36fc7695u,
                                  0x7879462eu, 0x666ea36fu, 0x9a07df2fu, 0x0e0a77c1u};  // 2^256 mod r
 __constant__ uint32_t kR2[8] = {0xae216da7u, 0x1bb8e645u, 0xe35c59e3u, 0x53fe3ab1u,
                                 0x53bb8085u, 0x8c49833du, 0x7f4e44a5u, 0x0216d0b1u};  // 2^512 mod r
-constexpr uint32_t kNP = 0xefffffffu;  // -r^-1 mod 2^32
 
-__device__ __forceinline__ bool geq_r(const uint32_t* t) {
-#pragma unroll
-    for (int i = 7; i >= 0; i--) {
-        if (t[i] > kR[i]) return true;
-        if (t[i] < kR[i]) return false;
-    }
-    return true;
-}
-__device__ __forceinline__ void sub_r(uint32_t* t) {
-    uint64_t br = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const uint64_t d = (uint64_t)t[i] - kR[i] - br;
-        t[i] = (uint32_t)d;
-        br = (d >> 63) & 1;
-    }
-}
 __device__ __forceinline__ Fr zero() {
     Fr z;
 #pragma unroll
@@ -46,73 +29,154 @@ __device__ __forceinline__ Fr one() {
     for (int i = 0; i < 8; i++) z.l[i] = kOne[i];
     return z;
 }
+// Field operations on canonical Montgomery forms (< r) as PTX carry chains (add.cc/addc,
+// mad.lo.cc/madc.hi.cc); each asm block holds a whole chain, so no carry flag crosses
+// statements.  The modulus limbs are immediates.
+
+// x - r with a borrow chain; returns the borrow-out word (0xffffffff when x < r).
+__device__ __forceinline__ uint32_t minus_r(const uint32_t* x, uint32_t* d) {
+    uint32_t bw;
+    asm("sub.cc.u32 %0, %9, 0xf0000001;\n\t"
+        "subc.cc.u32 %1, %10, 0x43e1f593;\n\t"
+        "subc.cc.u32 %2, %11, 0x79b97091;\n\t"
+        "subc.cc.u32 %3, %12, 0x2833e848;\n\t"
+        "subc.cc.u32 %4, %13, 0x8181585d;\n\t"
+        "subc.cc.u32 %5, %14, 0xb85045b6;\n\t"
+        "subc.cc.u32 %6, %15, 0xe131a029;\n\t"
+        "subc.cc.u32 %7, %16, 0x30644e72;\n\t"
+        "subc.u32 %8, 0, 0;"
+        : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]), "=r"(bw)
+        : "r"(x[0]), "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]));
+    return bw;
+}
+
 __device__ __forceinline__ Fr add(const Fr& a, const Fr& b) {
-    Fr s;
-    uint64_t c = 0;
+    uint32_t s[8], d[8];
+    // a + b < 2r < 2^255: no carry out of the top limb
+    asm("add.cc.u32 %0, %8, %16;\n\t"
+        "addc.cc.u32 %1, %9, %17;\n\t"
+        "addc.cc.u32 %2, %10, %18;\n\t"
+        "addc.cc.u32 %3, %11, %19;\n\t"
+        "addc.cc.u32 %4, %12, %20;\n\t"
+        "addc.cc.u32 %5, %13, %21;\n\t"
+        "addc.cc.u32 %6, %14, %22;\n\t"
+        "addc.u32 %7, %15, %23;"
+        : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7])
+        : "r"(a.l[0]), "r"(a.l[1]), "r"(a.l[2]), "r"(a.l[3]), "r"(a.l[4]), "r"(a.l[5]), "r"(a.l[6]), "r"(a.l[7]),
+          "r"(b.l[0]), "r"(b.l[1]), "r"(b.l[2]), "r"(b.l[3]), "r"(b.l[4]), "r"(b.l[5]), "r"(b.l[6]), "r"(b.l[7]));
+    const bool below = minus_r(s, d) != 0u;
+    Fr o;
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-        c += (uint64_t)a.l[i] + b.l[i];
-        s.l[i] = (uint32_t)c;
-        c >>= 32;
-    }
-    if (geq_r(s.l)) sub_r(s.l);  // a + b < 2r < 2^255: no carry out of the top limb
-    return s;
+    for (int i = 0; i < 8; i++) o.l[i] = below ? s[i] : d[i];
+    return o;
 }
 __device__ __forceinline__ Fr sub(const Fr& a, const Fr& b) {
-    Fr d;
-    uint64_t br = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const uint64_t x = (uint64_t)a.l[i] - b.l[i] - br;
-        d.l[i] = (uint32_t)x;
-        br = (x >> 63) & 1;
-    }
-    if (br) {
-        uint64_t c = 0;
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            c += (uint64_t)d.l[i] + kR[i];
-            d.l[i] = (uint32_t)c;
-            c >>= 32;
-        }
-    }
-    return d;
+    uint32_t d[8], bw;
+    asm("sub.cc.u32 %0, %9, %17;\n\t"
+        "subc.cc.u32 %1, %10, %18;\n\t"
+        "subc.cc.u32 %2, %11, %19;\n\t"
+        "subc.cc.u32 %3, %12, %20;\n\t"
+        "subc.cc.u32 %4, %13, %21;\n\t"
+        "subc.cc.u32 %5, %14, %22;\n\t"
+        "subc.cc.u32 %6, %15, %23;\n\t"
+        "subc.cc.u32 %7, %16, %24;\n\t"
+        "subc.u32 %8, 0, 0;"
+        : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]), "=r"(bw)
+        : "r"(a.l[0]), "r"(a.l[1]), "r"(a.l[2]), "r"(a.l[3]), "r"(a.l[4]), "r"(a.l[5]), "r"(a.l[6]), "r"(a.l[7]),
+          "r"(b.l[0]), "r"(b.l[1]), "r"(b.l[2]), "r"(b.l[3]), "r"(b.l[4]), "r"(b.l[5]), "r"(b.l[6]), "r"(b.l[7]));
+    // a < b: add r back (bw is all ones, masking r's limbs)
+    Fr o;
+    asm("{\n\t.reg .u32 m0, m1, m2, m3, m4, m5, m6, m7;\n\t"
+        "and.b32 m0, %16, 0xf0000001;\n\t"
+        "and.b32 m1, %16, 0x43e1f593;\n\t"
+        "and.b32 m2, %16, 0x79b97091;\n\t"
+        "and.b32 m3, %16, 0x2833e848;\n\t"
+        "and.b32 m4, %16, 0x8181585d;\n\t"
+        "and.b32 m5, %16, 0xb85045b6;\n\t"
+        "and.b32 m6, %16, 0xe131a029;\n\t"
+        "and.b32 m7, %16, 0x30644e72;\n\t"
+        "add.cc.u32 %0, %8, m0;\n\t"
+        "addc.cc.u32 %1, %9, m1;\n\t"
+        "addc.cc.u32 %2, %10, m2;\n\t"
+        "addc.cc.u32 %3, %11, m3;\n\t"
+        "addc.cc.u32 %4, %12, m4;\n\t"
+        "addc.cc.u32 %5, %13, m5;\n\t"
+        "addc.cc.u32 %6, %14, m6;\n\t"
+        "addc.u32 %7, %15, m7;\n\t"
+        "}"
+        : "=r"(o.l[0]), "=r"(o.l[1]), "=r"(o.l[2]), "=r"(o.l[3]), "=r"(o.l[4]), "=r"(o.l[5]), "=r"(o.l[6]),
+          "=r"(o.l[7])
+        : "r"(d[0]), "r"(d[1]), "r"(d[2]), "r"(d[3]), "r"(d[4]), "r"(d[5]), "r"(d[6]), "r"(d[7]), "r"(bw));
+    return o;
 }
-// Montgomery product a * b * 2^-256 mod r.
+
+// One CIOS step (Koc, Acar, Kaliski 1996): t += a * bi, then t += m * r with
+// m = t0 * (-r^-1) mod 2^32, which clears t0.  t0..t9 are %0..%9, a is %10..%17, bi %18.
+#define GKRGPU_BN_CIOS_STEP                      \
+    "{\n\t.reg .u32 m;\n\t"                      \
+    "mad.lo.cc.u32 %0, %10, %18, %0;\n\t"        \
+    "madc.lo.cc.u32 %1, %11, %18, %1;\n\t"       \
+    "madc.lo.cc.u32 %2, %12, %18, %2;\n\t"       \
+    "madc.lo.cc.u32 %3, %13, %18, %3;\n\t"       \
+    "madc.lo.cc.u32 %4, %14, %18, %4;\n\t"       \
+    "madc.lo.cc.u32 %5, %15, %18, %5;\n\t"       \
+    "madc.lo.cc.u32 %6, %16, %18, %6;\n\t"       \
+    "madc.lo.cc.u32 %7, %17, %18, %7;\n\t"       \
+    "addc.cc.u32 %8, %8, 0;\n\t"                 \
+    "addc.u32 %9, 0, 0;\n\t"                     \
+    "mad.hi.cc.u32 %1, %10, %18, %1;\n\t"        \
+    "madc.hi.cc.u32 %2, %11, %18, %2;\n\t"       \
+    "madc.hi.cc.u32 %3, %12, %18, %3;\n\t"       \
+    "madc.hi.cc.u32 %4, %13, %18, %4;\n\t"       \
+    "madc.hi.cc.u32 %5, %14, %18, %5;\n\t"       \
+    "madc.hi.cc.u32 %6, %15, %18, %6;\n\t"       \
+    "madc.hi.cc.u32 %7, %16, %18, %7;\n\t"       \
+    "madc.hi.cc.u32 %8, %17, %18, %8;\n\t"       \
+    "addc.u32 %9, %9, 0;\n\t"                    \
+    "mul.lo.u32 m, %0, 0xefffffff;\n\t"          \
+    "mad.lo.cc.u32 %0, m, 0xf0000001, %0;\n\t"   \
+    "madc.lo.cc.u32 %1, m, 0x43e1f593, %1;\n\t"  \
+    "madc.lo.cc.u32 %2, m, 0x79b97091, %2;\n\t"  \
+    "madc.lo.cc.u32 %3, m, 0x2833e848, %3;\n\t"  \
+    "madc.lo.cc.u32 %4, m, 0x8181585d, %4;\n\t"  \
+    "madc.lo.cc.u32 %5, m, 0xb85045b6, %5;\n\t"  \
+    "madc.lo.cc.u32 %6, m, 0xe131a029, %6;\n\t"  \
+    "madc.lo.cc.u32 %7, m, 0x30644e72, %7;\n\t"  \
+    "addc.cc.u32 %8, %8, 0;\n\t"                 \
+    "addc.u32 %9, %9, 0;\n\t"                    \
+    "mad.hi.cc.u32 %1, m, 0xf0000001, %1;\n\t"   \
+    "madc.hi.cc.u32 %2, m, 0x43e1f593, %2;\n\t"  \
+    "madc.hi.cc.u32 %3, m, 0x79b97091, %3;\n\t"  \
+    "madc.hi.cc.u32 %4, m, 0x2833e848, %4;\n\t"  \
+    "madc.hi.cc.u32 %5, m, 0x8181585d, %5;\n\t"  \
+    "madc.hi.cc.u32 %6, m, 0xb85045b6, %6;\n\t"  \
+    "madc.hi.cc.u32 %7, m, 0xe131a029, %7;\n\t"  \
+    "madc.hi.cc.u32 %8, m, 0x30644e72, %8;\n\t"  \
+    "addc.u32 %9, %9, 0;\n\t"                    \
+    "}"
+
+// Montgomery product a * b * 2^-256 mod r (inputs < r, output < r).
 __device__ __forceinline__ Fr mul(const Fr& a, const Fr& b) {
-    uint32_t t[10];
-#pragma unroll
-    for (int i = 0; i < 10; i++) t[i] = 0u;
+    uint32_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0, t8 = 0, t9 = 0;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-        uint64_t c = 0;
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            c += (uint64_t)a.l[j] * b.l[i] + t[j];
-            t[j] = (uint32_t)c;
-            c >>= 32;
-        }
-        c += t[8];
-        t[8] = (uint32_t)c;
-        t[9] = (uint32_t)(c >> 32);
-        const uint32_t m = t[0] * kNP;
-        c = ((uint64_t)m * kR[0] + t[0]) >> 32;
-#pragma unroll
-        for (int j = 1; j < 8; j++) {
-            c += (uint64_t)m * kR[j] + t[j];
-            t[j - 1] = (uint32_t)c;
-            c >>= 32;
-        }
-        c += t[8];
-        t[7] = (uint32_t)c;
-        t[8] = t[9] + (uint32_t)(c >> 32);
+        asm(GKRGPU_BN_CIOS_STEP
+            : "+r"(t0), "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8), "+r"(t9)
+            : "r"(a.l[0]), "r"(a.l[1]), "r"(a.l[2]), "r"(a.l[3]), "r"(a.l[4]), "r"(a.l[5]), "r"(a.l[6]),
+              "r"(a.l[7]), "r"(b.l[i]));
+        // divide by 2^32: t0 is zero
+        t0 = t1; t1 = t2; t2 = t3; t3 = t4; t4 = t5; t5 = t6; t6 = t7; t7 = t8; t8 = t9; t9 = 0;
     }
-    Fr r;
+    // t < 2r < 2^255, so t8 is 0: one conditional subtraction of r
+    const uint32_t t[8] = {t0, t1, t2, t3, t4, t5, t6, t7};
+    uint32_t d[8];
+    const bool below = minus_r(t, d) != 0u;
+    Fr o;
 #pragma unroll
-    for (int i = 0; i < 8; i++) r.l[i] = t[i];
-    if (t[8] || geq_r(r.l)) sub_r(r.l);
-    return r;
+    for (int i = 0; i < 8; i++) o.l[i] = below ? t[i] : d[i];
+    return o;
 }
+#undef GKRGPU_BN_CIOS_STEP
 __device__ __forceinline__ Fr from_mont(const Fr& a) {
     Fr u = zero();
     u.l[0] = 1u;
@@ -126,43 +190,60 @@ __device__ __forceinline__ Fr to_mont(const Fr& a) {
 }
 __device__ __forceinline__ Fr fold(const Fr& a, const Fr& b, const Fr& r) { return add(a, mul(sub(b, a), r)); }
 
-// T = sum_k s[k] 2^(32k) (the 64-bit limb sums of many Montgomery values) reduced mod r:
-// REDC(T) = T 2^-256, then a Montgomery product with 2^512 mod r gives T mod r.
-__device__ Fr reduce_sums(const unsigned long long* s) {
-    uint32_t t[16];
+// The canonical value of a sum of Montgomery forms given as 64-bit limb sums:
+// T = sum_k s[k] 2^(32k) is the sum of the x_i R (R = 2^256), so REDC(T) = T R^-1 mod r is
+// sum x_i, already canonical after one conditional subtraction (T < 2^266 keeps
+// REDC(T) < 2r).  Eight reduction steps of CIOS on a ten-word window.
+__device__ __forceinline__ Fr redc_sums(const unsigned long long* s) {
+    uint32_t t0, t1, t2, t3, t4, t5, t6, t7, t8, t9;
+    {
+        uint32_t w[10];
+        unsigned long long c = 0;
 #pragma unroll
-    for (int i = 0; i < 16; i++) t[i] = 0u;
-    unsigned long long c = 0;
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const unsigned long long lo = c + (s[k] & 0xffffffffull);
-        t[k] = (uint32_t)lo;
-        c = (lo >> 32) + (s[k] >> 32);
+        for (int k = 0; k < 8; k++) {
+            const unsigned long long lo = c + (s[k] & 0xffffffffull);
+            w[k] = (uint32_t)lo;
+            c = (lo >> 32) + (s[k] >> 32);
+        }
+        w[8] = (uint32_t)c;
+        w[9] = (uint32_t)(c >> 32);
+        t0 = w[0]; t1 = w[1]; t2 = w[2]; t3 = w[3]; t4 = w[4];
+        t5 = w[5]; t6 = w[6]; t7 = w[7]; t8 = w[8]; t9 = w[9];
     }
-    t[8] = (uint32_t)c;
-    t[9] = (uint32_t)(c >> 32);
+#pragma unroll
     for (int i = 0; i < 8; i++) {
-        const uint32_t m = t[i] * kNP;
-        uint64_t cc = 0;
-        for (int j = 0; j < 8; j++) {
-            cc += (uint64_t)m * kR[j] + t[i + j];
-            t[i + j] = (uint32_t)cc;
-            cc >>= 32;
-        }
-        for (int j = i + 8; j < 16 && cc; j++) {
-            cc += t[j];
-            t[j] = (uint32_t)cc;
-            cc >>= 32;
-        }
+        asm("{\n\t.reg .u32 m;\n\t"
+            "mul.lo.u32 m, %0, 0xefffffff;\n\t"
+            "mad.lo.cc.u32 %0, m, 0xf0000001, %0;\n\t"
+            "madc.lo.cc.u32 %1, m, 0x43e1f593, %1;\n\t"
+            "madc.lo.cc.u32 %2, m, 0x79b97091, %2;\n\t"
+            "madc.lo.cc.u32 %3, m, 0x2833e848, %3;\n\t"
+            "madc.lo.cc.u32 %4, m, 0x8181585d, %4;\n\t"
+            "madc.lo.cc.u32 %5, m, 0xb85045b6, %5;\n\t"
+            "madc.lo.cc.u32 %6, m, 0xe131a029, %6;\n\t"
+            "madc.lo.cc.u32 %7, m, 0x30644e72, %7;\n\t"
+            "addc.cc.u32 %8, %8, 0;\n\t"
+            "addc.u32 %9, %9, 0;\n\t"
+            "mad.hi.cc.u32 %1, m, 0xf0000001, %1;\n\t"
+            "madc.hi.cc.u32 %2, m, 0x43e1f593, %2;\n\t"
+            "madc.hi.cc.u32 %3, m, 0x79b97091, %3;\n\t"
+            "madc.hi.cc.u32 %4, m, 0x2833e848, %4;\n\t"
+            "madc.hi.cc.u32 %5, m, 0x8181585d, %5;\n\t"
+            "madc.hi.cc.u32 %6, m, 0xb85045b6, %6;\n\t"
+            "madc.hi.cc.u32 %7, m, 0xe131a029, %7;\n\t"
+            "madc.hi.cc.u32 %8, m, 0x30644e72, %8;\n\t"
+            "addc.u32 %9, %9, 0;\n\t"
+            "}"
+            : "+r"(t0), "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8), "+r"(t9));
+        t0 = t1; t1 = t2; t2 = t3; t3 = t4; t4 = t5; t5 = t6; t6 = t7; t7 = t8; t8 = t9; t9 = 0;
     }
-    Fr x;
+    const uint32_t t[8] = {t0, t1, t2, t3, t4, t5, t6, t7};
+    uint32_t d[8];
+    const bool below = minus_r(t, d) != 0u;
+    Fr o;
 #pragma unroll
-    for (int i = 0; i < 8; i++) x.l[i] = t[8 + i];
-    if (geq_r(x.l)) sub_r(x.l);
-    Fr r2;
-#pragma unroll
-    for (int i = 0; i < 8; i++) r2.l[i] = kR2[i];
-    return mul(x, r2);
+    for (int i = 0; i < 8; i++) o.l[i] = below ? t[i] : d[i];
+    return o;
 }
 
 __device__ __forceinline__ Fr ldf(const uint32_t* __restrict__ base, uint64_t row, uint32_t N, uint32_t lane) {
@@ -207,18 +288,38 @@ __device__ __forceinline__ Tile tile(const GeoBn& g) {
 // C components per thread -> shared-memory sum over the CTA's row slices -> 64-bit
 // atomic adds per limb -> the last CTA of the lane group hands its lanes to fin(lane).
 template <int C, class Fin>
-__device__ __forceinline__ void reduce_bn(const Fr (&acc)[C], const GeoBn& g, bool active, RedBn red, Fin fin) {
+__device__ __forceinline__ void reduce_bn(Fr (&acc)[C], const GeoBn& g, bool active, RedBn red, Fin fin) {
     extern __shared__ uint32_t smem[];
     const uint32_t tid = threadIdx.x, B = blockDim.x;
+    uint32_t rows = g.rps;
+    if (g.tpr < 32 && (g.tpr & (g.tpr - 1)) == 0) {
+        // power-of-two tile below a warp (every thread active): first fold the warp's row
+        // slices together with shuffles, leaving one row per warp
+        for (uint32_t off = g.tpr; off < 32; off <<= 1)
 #pragma unroll
-    for (int c = 0; c < C; c++)
+            for (int c = 0; c < C; c++) {
+                Fr o;
 #pragma unroll
-        for (int k = 0; k < 8; k++) smem[(c * 8 + k) * B + tid] = active ? acc[c].l[k] : 0u;
+                for (int k = 0; k < 8; k++) o.l[k] = __shfl_xor_sync(0xffffffffu, acc[c].l[k], off);
+                acc[c] = add(acc[c], o);
+            }
+        rows = B / 32;
+        if ((tid & 31) < g.tpr)
+#pragma unroll
+            for (int c = 0; c < C; c++)
+#pragma unroll
+                for (int k = 0; k < 8; k++) smem[(c * 8 + k) * B + (tid >> 5) * g.tpr + (tid & 31)] = acc[c].l[k];
+    } else {
+#pragma unroll
+        for (int c = 0; c < C; c++)
+#pragma unroll
+            for (int k = 0; k < 8; k++) smem[(c * 8 + k) * B + tid] = active ? acc[c].l[k] : 0u;
+    }
     __syncthreads();
     for (uint32_t o = tid; o < (uint32_t)C * g.tpr; o += B) {
         const uint32_t c = o / g.tpr, q = o - c * g.tpr;
         Fr s = zero();
-        for (uint32_t r = 0; r < g.rps; r++) {
+        for (uint32_t r = 0; r < rows; r++) {
             Fr x;
 #pragma unroll
             for (int k = 0; k < 8; k++) x.l[k] = smem[(c * 8 + k) * B + r * g.tpr + q];
@@ -244,6 +345,7 @@ __device__ __forceinline__ void reduce_bn(const Fr (&acc)[C], const GeoBn& g, bo
     }
 }
 
+// Canonical total of component c of one lane; leaves its accumulators zeroed.
 __device__ __forceinline__ Fr take(const RedBn& red, uint32_t c, uint32_t N, uint32_t lane) {
     unsigned long long s[8];
     unsigned long long* p = &red.acc[((size_t)c * N + lane) * 8];
@@ -252,10 +354,11 @@ __device__ __forceinline__ Fr take(const RedBn& red, uint32_t c, uint32_t N, uin
         s[k] = __ldcg(p + k);
         p[k] = 0ull;
     }
-    return reduce_sums(s);
+    return redc_sums(s);
 }
 
-// Evaluations at 0, 1, 2 (canonical) of one lane; phase two multiplies by vx (Montgomery).
+// Evaluations at 0, 1, 2 (canonical) of one lane; phase two multiplies by vx: a Montgomery
+// product of a canonical value with vx's Montgomery form is the canonical product.
 struct RoundFinBn {
     RedBn red;
     uint32_t* out;  // 3 x N x 8 limbs, canonical
@@ -273,9 +376,9 @@ struct RoundFinBn {
             p1 = mul(p1, x);
             p2 = mul(p2, x);
         }
-        stf(out, 0, N, lane, from_mont(p0));
-        stf(out, 1, N, lane, from_mont(p1));
-        stf(out, 2, N, lane, from_mont(p2));
+        stf(out, 0, N, lane, p0);
+        stf(out, 1, N, lane, p1);
+        stf(out, 2, N, lane, p2);
     }
 };
 
@@ -283,7 +386,7 @@ struct CopyFinBn {
     RedBn red;
     uint32_t* out;  // N x 8 limbs, canonical
     uint32_t N;
-    __device__ void operator()(uint32_t lane) const { stf(out, 0, N, lane, from_mont(take(red, 0, N, lane))); }
+    __device__ void operator()(uint32_t lane) const { stf(out, 0, N, lane, take(red, 0, N, lane)); }
 };
 
 __device__ __forceinline__ void accum(Fr (&acc)[3], const Fr& f0, const Fr& f1, const Fr& h0, const Fr& h1) {
@@ -298,7 +401,8 @@ __global__ void k_load(const uint32_t* __restrict__ canon, uint32_t* __restrict_
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         Fr x = lds(reinterpret_cast<const Fr*>(canon), i);
-        if (geq_r(x.l)) {
+        uint32_t d[8];
+        if (minus_r(x.l, d) == 0u) {  // no borrow: x >= r
             atomicOr(bad, 1u);
             x = zero();
         }
@@ -342,26 +446,55 @@ __global__ void __launch_bounds__(256) k_evaluate(const uint32_t* __restrict__ i
     }
 }
 
-__global__ void k_eq(Fr* __restrict__ out, EqArgsBn a) {
-    const uint64_t size = 1ull << a.nvars;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t z = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; z < size; z += stride) {
-        Fr e1, e2;
+// eq(r, z) * f = f * prod_t (bit t of z ? r_t : 1 - r_t) for z < 2^nvars (two tables summed
+// when has_r2).  Split at bit h = min(nvars, 8): every CTA builds the 2^h-entry table of the
+// low bits in shared memory by doubling, then each chunk of 2^h consecutive z shares one
+// high-bit product, so an entry costs one multiplication (two with has_r2).
+constexpr uint32_t kEqLowBits = 8;
+
+__device__ __forceinline__ Fr eq_factor(const uint32_t (*r)[8], uint32_t t, bool bit) {
+    Fr x;
 #pragma unroll
-        for (int k = 0; k < 8; k++) { e1.l[k] = a.f1[k]; e2.l[k] = a.f2[k]; }
-        for (uint32_t t = 0; t < a.nvars; t++) {
-            Fr r1;
-#pragma unroll
-            for (int k = 0; k < 8; k++) r1.l[k] = a.r1[t][k];
-            e1 = mul(e1, ((z >> t) & 1) ? r1 : sub(one(), r1));
-            if (a.has_r2) {
-                Fr r2;
-#pragma unroll
-                for (int k = 0; k < 8; k++) r2.l[k] = a.r2[t][k];
-                e2 = mul(e2, ((z >> t) & 1) ? r2 : sub(one(), r2));
-            }
+    for (int k = 0; k < 8; k++) x.l[k] = r[t][k];
+    return bit ? x : sub(one(), x);
+}
+
+__global__ void __launch_bounds__(256) k_eq(Fr* __restrict__ out, EqArgsBn a) {
+    __shared__ Fr lo[2][1u << kEqLowBits];
+    __shared__ Fr hi[2];
+    const uint32_t h = a.nvars < kEqLowBits ? a.nvars : kEqLowBits;
+    const uint32_t L = 1u << h;
+    const uint32_t tabs = a.has_r2 ? 2u : 1u;
+    if (threadIdx.x < tabs) lo[threadIdx.x][0] = one();
+    __syncthreads();
+    for (uint32_t t = 0; t < h; t++) {
+        const uint32_t half = 1u << t;
+        for (uint32_t x = threadIdx.x; x < half * tabs; x += blockDim.x) {
+            const uint32_t k = x >> t, y = x & (half - 1);
+            const uint32_t(*r)[8] = k ? a.r2 : a.r1;
+            const Fr v = lo[k][y];
+            lo[k][y + half] = mul(v, eq_factor(r, t, true));
+            lo[k][y] = mul(v, eq_factor(r, t, false));
         }
-        sts(out, z, a.has_r2 ? add(e1, e2) : e1);
+        __syncthreads();
+    }
+    const uint64_t chunks = 1ull << (a.nvars - h);
+    for (uint64_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+        if (threadIdx.x < tabs) {
+            const uint32_t(*r)[8] = threadIdx.x ? a.r2 : a.r1;
+            Fr e;
+#pragma unroll
+            for (int k = 0; k < 8; k++) e.l[k] = threadIdx.x ? a.f2[k] : a.f1[k];
+            for (uint32_t t = h; t < a.nvars; t++) e = mul(e, eq_factor(r, t, (c >> (t - h)) & 1));
+            hi[threadIdx.x] = e;
+        }
+        __syncthreads();
+        for (uint32_t x = threadIdx.x; x < L; x += blockDim.x) {
+            Fr e = mul(lo[0][x], hi[0]);
+            if (a.has_r2) e = add(e, mul(lo[1][x], hi[1]));
+            sts(out, (c << h) + x, e);
+        }
+        __syncthreads();
     }
 }
 
@@ -414,36 +547,59 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrsBn p, uint64_t npairs, c
     Fr acc[3] = {zero(), zero(), zero()};
     const Fr* hs = reinterpret_cast<const Fr*>(p.hsrc);
     Fr* hd = reinterpret_cast<Fr*>(p.hdst);
-    if (t.active) {
-        for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
-            Fr f0, f1, h0, h1;
-            if (FOLD) {
+    // Phase two folds the lane-independent scalar table: with a power-of-two row tile of at
+    // least 2, the threads of a row slice within a warp share it (two of them fold, the
+    // others take the results by shuffle), so the loop runs warp-uniformly.
+    const bool share = !LANE_HG && FOLD && g.tpr >= 2 && (g.tpr & (g.tpr - 1)) == 0;
+    const uint32_t grp = g.tpr < 32 ? g.tpr : 32;
+    const uint32_t gq = threadIdx.x & (grp - 1);
+    const uint32_t q = threadIdx.x % g.tpr;
+    const uint64_t stride = (uint64_t)gridDim.x * g.rps;
+    for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs;; i += stride) {
+        const bool valid = t.active && i < npairs;
+        if (share) {
+            if (!__any_sync(0xffffffffu, valid)) break;
+        } else if (!valid) {
+            break;
+        }
+        Fr f0 = zero(), f1 = zero(), h0, h1;
+        if (FOLD) {
+            if (valid) {
                 f0 = fold(ldf(p.fsrc, 4 * i, g.N, t.q), ldf(p.fsrc, 4 * i + 1, g.N, t.q), r);
                 f1 = fold(ldf(p.fsrc, 4 * i + 2, g.N, t.q), ldf(p.fsrc, 4 * i + 3, g.N, t.q), r);
                 stf(p.fdst, 2 * i, g.N, t.q, f0);
                 stf(p.fdst, 2 * i + 1, g.N, t.q, f1);
-                if (LANE_HG) {
-                    h0 = fold(ldf(p.hsrc, 4 * i, g.N, t.q), ldf(p.hsrc, 4 * i + 1, g.N, t.q), r);
-                    h1 = fold(ldf(p.hsrc, 4 * i + 2, g.N, t.q), ldf(p.hsrc, 4 * i + 3, g.N, t.q), r);
-                    stf(p.hdst, 2 * i, g.N, t.q, h0);
-                    stf(p.hdst, 2 * i + 1, g.N, t.q, h1);
-                } else {
-                    h0 = fold(lds(hs, 4 * i), lds(hs, 4 * i + 1), r);
-                    h1 = fold(lds(hs, 4 * i + 2), lds(hs, 4 * i + 3), r);
-                    // the scalar table is shared by all lanes: lane 0 of group 0 writes it
-                    if (threadIdx.x % g.tpr == 0 && blockIdx.y == 0) {
-                        sts(hd, 2 * i, h0);
-                        sts(hd, 2 * i + 1, h1);
-                    }
+            }
+            if (LANE_HG) {
+                h0 = fold(ldf(p.hsrc, 4 * i, g.N, t.q), ldf(p.hsrc, 4 * i + 1, g.N, t.q), r);
+                h1 = fold(ldf(p.hsrc, 4 * i + 2, g.N, t.q), ldf(p.hsrc, 4 * i + 3, g.N, t.q), r);
+                stf(p.hdst, 2 * i, g.N, t.q, h0);
+                stf(p.hdst, 2 * i + 1, g.N, t.q, h1);
+            } else if (share) {
+                Fr mine = zero();
+                if (valid && gq < 2) mine = fold(lds(hs, 4 * i + 2 * gq), lds(hs, 4 * i + 2 * gq + 1), r);
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    h0.l[k] = __shfl_sync(0xffffffffu, mine.l[k], 0, grp);
+                    h1.l[k] = __shfl_sync(0xffffffffu, mine.l[k], 1, grp);
                 }
             } else {
-                f0 = ldf(p.fsrc, 2 * i, g.N, t.q);
-                f1 = ldf(p.fsrc, 2 * i + 1, g.N, t.q);
-                h0 = lds(hs, 2 * i);
-                h1 = lds(hs, 2 * i + 1);
+                h0 = fold(lds(hs, 4 * i), lds(hs, 4 * i + 1), r);
+                h1 = fold(lds(hs, 4 * i + 2), lds(hs, 4 * i + 3), r);
             }
-            accum(acc, f0, f1, h0, h1);
+            // the scalar table is shared by all lanes: the first thread of the row slice in
+            // lane group 0 writes it
+            if (!LANE_HG && valid && q == 0 && blockIdx.y == 0) {
+                sts(hd, 2 * i, h0);
+                sts(hd, 2 * i + 1, h1);
+            }
+        } else {
+            f0 = ldf(p.fsrc, 2 * i, g.N, t.q);
+            f1 = ldf(p.fsrc, 2 * i + 1, g.N, t.q);
+            h0 = lds(hs, 2 * i);
+            h1 = lds(hs, 2 * i + 1);
         }
+        if (valid) accum(acc, f0, f1, h0, h1);
     }
     reduce_bn<3>(acc, g, t.active, red, RoundFinBn{red, evals_out, LANE_HG ? nullptr : vx, g.N});
 }
@@ -509,7 +665,8 @@ cudaError_t launch_evaluate(const uint32_t* in, uint32_t* out, uint64_t O, const
 }
 
 cudaError_t launch_eq(Fr* out, const EqArgsBn& a, cudaStream_t s) {
-    k_eq<<<grid1(1ull << a.nvars), 256, 0, s>>>(out, a);
+    const uint64_t chunks = 1ull << (a.nvars > kEqLowBits ? a.nvars - kEqLowBits : 0);
+    k_eq<<<(uint32_t)(chunks < 152ull * 4 ? chunks : 152ull * 4), 256, 0, s>>>(out, a);
     return cudaGetLastError();
 }
 
