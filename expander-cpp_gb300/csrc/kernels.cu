@@ -25,7 +25,8 @@ namespace gkrgpu {
 
 const char* const kKernelNames[K_NUM_KERNELS] = {"check_canonical", "evaluate", "eq_table", "gate_weights",
                                                  "hg_build_round0", "round_fold_lane", "round_fold_scalar",
-                                                 "phase2_s_build", "weighted_row_sum", "bn254_load",
+                                                 "phase2_s_build", "weighted_row_sum", "hg_rebuild_round1",
+                                                 "bn254_load",
                                                  "bn254_evaluate", "bn254_eq_table", "bn254_gate_weights",
                                                  "bn254_hg_build_round0", "bn254_round_fold_lane",
                                                  "bn254_round_fold_scalar", "bn254_phase2_s_build",
@@ -249,7 +250,9 @@ __device__ __forceinline__ void accum_pair(uint32_t (&acc)[3][4], const uint32_t
 
 // ---------------------------------------------------------------- phase one: hg build + round 0
 // For each pair (x0, x1) = (2i, 2i+1): hg_j[x] = a_j[x] + sum over mul gates (x, y, k) of
-// v[y] * w_j[k], written for the later folds, then the round-0 sums of v(x) hg_j(x).
+// v[y] * w_j[k], then the round-0 sums of v(x) hg_j(x).  The table is written only when
+// hg0 is given: the prover rebuilds it inside round 1 (k_hg_round1) instead, which costs
+// the gathers again but saves writing and re-reading R full-width tables.
 // All repetitions in one thread: each gathered v[y] row serves the R weights.
 template <int R>
 __global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ v, uint64_t I,
@@ -282,8 +285,9 @@ __global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ 
 #pragma unroll
                         for (int l = 0; l < 4; l++) h[s][j][l] = add(h[s][j][l], mul(comp(vy, l), comp(w, j)));
                 }
+                if (hg0)
 #pragma unroll
-                for (int j = 0; j < R; j++) st4(hg[j], x, g.N, t.lane0, mk4(h[s][j]));
+                    for (int j = 0; j < R; j++) st4(hg[j], x, g.N, t.lane0, mk4(h[s][j]));
             }
             const uint4 v0 = ld4(v, 2 * i, g.N, t.lane0), v1 = ld4(v, 2 * i + 1, g.N, t.lane0);
 #pragma unroll
@@ -295,6 +299,76 @@ __global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ 
                     acc[3 * j + 1][l] = add(acc[3 * j + 1][l], mul(f1, h[1][j][l]));
                     acc[3 * j + 2][l] = add(acc[3 * j + 2][l], mul(add(f0, f1), add(h[0][j][l], h[1][j][l])));
                 }
+        }
+    }
+    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R});
+}
+
+// ---------------------------------------------------------------- phase one, round 1
+// Round 1 with hg rebuilt rather than read: for each output pair i the four source rows
+// x = 4i..4i+3 get hg_j[x] = a_j[x] + sum over mul gates (x, y, k) of v[y] w_j[k] again,
+// and hg_j and the layer input are folded at r_j into rows 2i, 2i+1 of hdst_j / fdst_j
+// (what receive_challenge of round 0 would have left, sumcheck_helper.hpp:104-133), which
+// are stored and summed into the round-1 evaluations.  All repetitions in one thread, as in
+// k_hg_round0: each gathered v[y] row serves the R weights.  After the first half of a pair
+// only f and h of row 2i are kept (for the (f0 + f1)(h0 + h1) term).
+template <int R>
+__global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ v, uint64_t npairs,
+                                                   const uint32_t* __restrict__ mx_off, const uint4* __restrict__ mx_g,
+                                                   const uint4* __restrict__ a4, const uint4* __restrict__ w4,
+                                                   RoundPtrs p, Geo g, RedScratch red, uint32_t* evals_out) {
+    const TileIdx t = tile_idx(g);
+    uint32_t acc[3 * R][4] = {};
+    if (t.active) {
+        for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
+            uint32_t f0[R][4], h0[R][4];
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                uint32_t hx[2][R][4];
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    const uint64_t x = 4 * i + 2 * s + e;
+                    const uint4 a = __ldg(a4 + x);
+#pragma unroll
+                    for (int j = 0; j < R; j++)
+#pragma unroll
+                        for (int l = 0; l < 4; l++) hx[e][j][l] = comp(a, j);
+                    const uint32_t k0 = __ldg(mx_off + x), k1 = __ldg(mx_off + x + 1);
+                    for (uint32_t k = k0; k < k1; k++) {
+                        const uint32_t y = __ldg(&mx_g[k].x);
+                        const uint4 w = __ldg(w4 + k);
+                        const uint4 vy = ld4(v, y, g.N, t.lane0);
+#pragma unroll
+                        for (int j = 0; j < R; j++)
+#pragma unroll
+                            for (int l = 0; l < 4; l++) hx[e][j][l] = add(hx[e][j][l], mul(comp(vy, l), comp(w, j)));
+                    }
+                }
+                const uint4 v0 = ld4(v, 4 * i + 2 * s, g.N, t.lane0), v1 = ld4(v, 4 * i + 2 * s + 1, g.N, t.lane0);
+#pragma unroll
+                for (int j = 0; j < R; j++) {
+                    const uint32_t r = p.r[j];
+                    uint32_t f[4], h[4];
+#pragma unroll
+                    for (int l = 0; l < 4; l++) {
+                        f[l] = fold(comp(v0, l), comp(v1, l), r);
+                        h[l] = fold(hx[0][j][l], hx[1][j][l], r);
+                    }
+                    st4(p.fdst[j], 2 * i + s, g.N, t.lane0, mk4(f));
+                    st4(p.hdst[j], 2 * i + s, g.N, t.lane0, mk4(h));
+#pragma unroll
+                    for (int l = 0; l < 4; l++) {
+                        if (s == 0) {
+                            acc[3 * j][l] = add(acc[3 * j][l], mul(f[l], h[l]));
+                            f0[j][l] = f[l];
+                            h0[j][l] = h[l];
+                        } else {
+                            acc[3 * j + 1][l] = add(acc[3 * j + 1][l], mul(f[l], h[l]));
+                            acc[3 * j + 2][l] = add(acc[3 * j + 2][l], mul(add(f0[j][l], f[l]), add(h0[j][l], h[l])));
+                        }
+                    }
+                }
+            }
         }
     }
     reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R});
@@ -550,6 +624,19 @@ cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint
         case 1: k_hg_round0<1><<<sh.grid, sh.block, sh.smem, s>>>(v, I, mx_off, mx_g, a4, w4, hg[0], hg[1], hg[2], g, red, evals_out); break;
         case 2: k_hg_round0<2><<<sh.grid, sh.block, sh.smem, s>>>(v, I, mx_off, mx_g, a4, w4, hg[0], hg[1], hg[2], g, red, evals_out); break;
         case 3: k_hg_round0<3><<<sh.grid, sh.block, sh.smem, s>>>(v, I, mx_off, mx_g, a4, w4, hg[0], hg[1], hg[2], g, red, evals_out); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* mx_off, const uint4* mx_g,
+                             const uint4* a4, const uint4* w4, const RoundPtrs& p, const Geo& g, uint32_t block,
+                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
+    LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
+    switch (reps) {
+        case 1: k_hg_round1<1><<<sh.grid, sh.block, sh.smem, s>>>(v, npairs, mx_off, mx_g, a4, w4, p, g, red, evals_out); break;
+        case 2: k_hg_round1<2><<<sh.grid, sh.block, sh.smem, s>>>(v, npairs, mx_off, mx_g, a4, w4, p, g, red, evals_out); break;
+        case 3: k_hg_round1<3><<<sh.grid, sh.block, sh.smem, s>>>(v, npairs, mx_off, mx_g, a4, w4, p, g, red, evals_out); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

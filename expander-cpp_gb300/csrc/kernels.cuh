@@ -57,6 +57,7 @@ enum KernelId {
     K_ROUND_SCALAR,
     K_S_BUILD,
     K_WSUM,
+    K_HG_ROUND1,
     // BN254 kernels (bn254.cuh)
     K_BN_LOAD,
     K_BN_EVALUATE,
@@ -86,6 +87,11 @@ cudaError_t launch_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* 
                            cudaStream_t s);
 cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint32_t* mx_off, const uint4* mx_g,
                              const uint4* a4, const uint4* w4, uint32_t* const hg[3], const Geo& g, uint32_t block,
+                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
+// Phase-one round 1 rebuilding hg from the gate weights (no stored hg table): outputs
+// p.fdst[j] / p.hdst[j] (I/2 rows each), challenges p.r[j]; npairs = I/4.
+cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* mx_off, const uint4* mx_g,
+                             const uint4* a4, const uint4* w4, const RoundPtrs& p, const Geo& g, uint32_t block,
                              uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
 cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold, const RoundPtrs& p, uint64_t npairs,
                          const uint32_t* vx, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,

@@ -641,7 +641,7 @@ struct Workspace {
         vals = (uint32_t*)take(rows * rowb);
         if (sumcheck) {
             for (int j = 0; j < R; j++) {
-                hg0[j] = (uint32_t*)take(maxI * rowb);
+                hg0[j] = (uint32_t*)take(std::max<uint64_t>(maxI / 4, 1) * rowb);  // rounds >= 2 only
                 hgA[j] = (uint32_t*)take(std::max<uint64_t>(maxI / 2, 1) * rowb);
                 fA[j] = (uint32_t*)take(std::max<uint64_t>(maxI / 2, 1) * rowb);
                 fB[j] = (uint32_t*)take(std::max<uint64_t>(maxI / 4, 1) * rowb);
@@ -826,8 +826,10 @@ struct Prover {
         c.launch(K_WEIGHTS, wb, [&] {
             return launch_weights(I, Ly.nmul, O, ws.eqc, Ly.mx_g, Ly.ax_off, Ly.ax_g, ws.a4, ws.w4, R, c.stream);
         });
-        uint32_t* hg[3] = {ws.hg0[0], ws.hg0[1], ws.hg0[2]};
-        const double hb = rb * (I + Ly.nmul + (double)R * I) + 32.0 * Ly.nmul + 20.0 * I;
+        // round 0 only reduces hg; round 1 rebuilds it (k_hg_round1), so no full-width hg
+        // table is ever written
+        uint32_t* hg[3] = {nullptr, nullptr, nullptr};
+        const double hb = rb * (I + Ly.nmul) + 32.0 * Ly.nmul + 20.0 * I;
         c.launch(K_HG_ROUND0, hb, [&] {
             return launch_hg_round0(R, v, I, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, hg, gk[K_HG_ROUND0], X.block,
                                     ck_ctas[K_HG_ROUND0], red_mapped(), c.evals_d(), c.stream);
@@ -850,13 +852,22 @@ struct Prover {
             }
             const uint64_t npairs = I >> (k + 1);
             const double S = 4.0 * npairs;
-            const double b = rb * ((k == 1 ? 1.0 : R) * S + R * S + R * S);
-            c.launch(K_ROUND_LANE, b, [&] {
-                return launch_round(R, k == 1, true, true, p, npairs, nullptr, gk[K_ROUND_LANE], X.block,
-                                    ck_ctas[K_ROUND_LANE], red_mapped(), c.evals_d(), c.stream);
-            });
+            int kid = K_ROUND_LANE;
+            if (k == 1) {
+                // hg rebuilt from the weights: v read once, the gathers again, f and hg halves out
+                kid = K_HG_ROUND1;
+                c.launch(K_HG_ROUND1, rb * (I + Ly.nmul + (double)R * I) + 32.0 * Ly.nmul + 20.0 * I, [&] {
+                    return launch_hg_round1(R, v, npairs, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, p, gk[K_HG_ROUND1],
+                                            X.block, ck_ctas[K_HG_ROUND1], red_mapped(), c.evals_d(), c.stream);
+                });
+            } else {
+                c.launch(K_ROUND_LANE, rb * 3.0 * R * S, [&] {
+                    return launch_round(R, false, true, true, p, npairs, nullptr, gk[K_ROUND_LANE], X.block,
+                                        ck_ctas[K_ROUND_LANE], red_mapped(), c.evals_d(), c.stream);
+                });
+            }
             const bool last = (k == n - 1);
-            fetch(groups(K_ROUND_LANE), last ? p.fdst : nullptr, false);
+            fetch(groups(kid), last ? p.fdst : nullptr, false);
             transcript_round(t, rx, k, last, true, vxh);
             for (int j = 0; j < R; j++) {
                 cur_f[j] = p.fdst[j];
@@ -1676,7 +1687,7 @@ int gkrgpu_autotune(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_c
         };
         const std::vector<int> kinds =
             bn ? std::vector<int>{K_BN_EVALUATE, K_BN_HG_ROUND0, K_BN_ROUND_LANE, K_BN_ROUND_SCALAR, K_BN_WSUM}
-               : std::vector<int>{K_EVALUATE, K_HG_ROUND0, K_ROUND_LANE, K_ROUND_SCALAR, K_WSUM};
+               : std::vector<int>{K_EVALUATE, K_HG_ROUND0, K_HG_ROUND1, K_ROUND_LANE, K_ROUND_SCALAR, K_WSUM};
         try {
             double ms[K_NUM_KERNELS];
             run(ms);  // warm-up: pool growth, first-launch costs

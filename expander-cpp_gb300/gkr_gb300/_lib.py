@@ -57,6 +57,11 @@ SIGNATURES = [
     ("gkrgpu_circuit_load", _I, [_P, _P, _I, ctypes.POINTER(_P)]),
     ("gkrgpu_circuit_load_field", _I, [_P, _P, _I, _I, ctypes.POINTER(_P)]),
     ("gkrgpu_circuit_field", _I, [_P]),
+    ("gkrgpu_circuit2_parse", _I, [_P, _U64, ctypes.POINTER(_P)]),
+    ("gkrgpu_extracted_parse", _I, [_P, _U64, _P, _U64, ctypes.POINTER(_P)]),
+    ("gkrgpu_parsed_layers", _I, [_P]),
+    ("gkrgpu_parsed_layer", _I, [_P, _I, _P]),
+    ("gkrgpu_parsed_free", None, [_P]),
     ("gkrgpu_circuit_free", None, [_P]),
     ("gkrgpu_proof_size", _U64, [_P, _U32, _I]),
     ("gkrgpu_value_rows", _U64, [_P, _I]),

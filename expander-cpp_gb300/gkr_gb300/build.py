@@ -22,7 +22,7 @@ if platform.machine() in ("aarch64", "arm64"):
     # ARMv8 SHA-2 instructions for the transcript hash (all Neoverse cores have them).
     CXXFLAGS.append("-march=armv8.2-a+crypto")
 
-SOURCES = ["kernels.cu", "prover.cu", "sha256.cpp", "noalloc.cu", "bn254.cu"]
+SOURCES = ["kernels.cu", "prover.cu", "sha256.cpp", "noalloc.cu", "bn254.cu", "circuit2.cpp"]
 HEADERS = ["kernels.cuh", "m31.cuh", "sha256.hpp", "transcript.hpp", "bn254.cuh", "bn254_prover.cuh", "fr_host.hpp"]
 
 

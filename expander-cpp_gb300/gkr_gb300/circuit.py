@@ -58,6 +58,54 @@ class Circuit:
         self.layers: list[CircuitLayer] = list(layers or [])
         self.input_values = None  # layers[0].input_layer_vals of the reference
 
+    @staticmethod
+    def from_circuit2(data) -> "Circuit":
+        """A CIRCUIT2 file (path or bytes) as CircuitRaw + Circuit::from_circuit_raw load it
+        (include/circuit/circuit_raw.hpp:511-568, include/circuit/circuit.hpp:217-251),
+        parsed by the native library (gkrgpu_circuit2_parse)."""
+        if not isinstance(data, (bytes, bytearray, memoryview)):
+            with open(data, "rb") as f:
+                data = f.read()
+        b = np.frombuffer(bytes(data), np.uint8)
+        return Circuit._from_parsed(lambda lib, h: lib.gkrgpu_circuit2_parse(b.ctypes.data if b.size else None,
+                                                                            b.size, h))
+
+    @staticmethod
+    def from_extracted(mul, add) -> "Circuit":
+        """The text gate lists of Circuit::load_extracted_gates (circuit.hpp:152-215): paths
+        or the file contents as str/bytes (gkrgpu_extracted_parse)."""
+        def text(x):
+            if isinstance(x, (bytes, bytearray)):
+                return bytes(x)
+            if isinstance(x, str) and ("\n" in x or not x.strip()):
+                return x.encode()
+            with open(x, "rb") as f:
+                return f.read()
+        m, a = text(mul), text(add)
+        return Circuit._from_parsed(lambda lib, h: lib.gkrgpu_extracted_parse(m, len(m), a, len(a), h))
+
+    @staticmethod
+    def _from_parsed(parse) -> "Circuit":
+        import ctypes
+
+        from . import _lib
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(parse(lib, ctypes.byref(h)))
+        try:
+            layers = []
+            for k in range(lib.gkrgpu_parsed_layers(h)):
+                d = _lib.LayerDesc()
+                _lib.check(lib.gkrgpu_parsed_layer(h, k, ctypes.byref(d)))
+                mul = np.ctypeslib.as_array(ctypes.cast(d.mul, ctypes.POINTER(ctypes.c_uint32)), (d.n_mul, 4)).copy() \
+                    if d.n_mul else None
+                add = np.ctypeslib.as_array(ctypes.cast(d.add, ctypes.POINTER(ctypes.c_uint32)), (d.n_add, 3)).copy() \
+                    if d.n_add else None
+                layers.append(CircuitLayer(d.nb_output_vars, d.nb_input_vars, mul, add))
+            return Circuit(layers)
+        finally:
+            lib.gkrgpu_parsed_free(h)
+
     def set_input(self, values) -> None:
         """Sets the circuit input: a (2^nb_input_vars(layer 0), N) array of canonical M31."""
         v = np.ascontiguousarray(values, dtype=np.uint32)

@@ -102,6 +102,27 @@ int gkrgpu_circuit_load_field(gkrgpu_ctx* ctx, const gkrgpu_layer_desc* layers, 
 /* Field of a loaded circuit (GKRGPU_FIELD_*), negative for a null circuit. */
 int gkrgpu_circuit_field(const gkrgpu_circuit* circuit);
 
+/* Circuit files of the reference, parsed on the host into layers ready for
+ * gkrgpu_circuit_load(_field).  The handle owns the gate arrays the layer descriptors point
+ * to; free it with gkrgpu_parsed_free after loading.
+ *
+ * gkrgpu_circuit2_parse: the binary CIRCUIT2 segment format (CircuitRaw::operator>>,
+ *   include/circuit/circuit_raw.hpp:511-568) flattened as Circuit::from_circuit_raw does
+ *   (include/circuit/circuit.hpp:217-251): segment trees expanded with their allocation
+ *   offsets, const gates dropped, layer sizes from the largest gate ids
+ *   (_compute_nb_vars, circuit.hpp:124-150), and every coefficient 1, because the
+ *   reference's M31 reader discards the 32 bytes it reads (include/field/M31.hpp:124-135).
+ * gkrgpu_extracted_parse: the text gate lists of Circuit::load_extracted_gates
+ *   (circuit.hpp:152-215), line i of each file being layer (lines - 1 - i).
+ * A malformed file gives GKRGPU_ERR_INVALID (the reference exits the process). */
+typedef struct gkrgpu_parsed gkrgpu_parsed;
+int gkrgpu_circuit2_parse(const uint8_t* bytes, uint64_t len, gkrgpu_parsed** out);
+int gkrgpu_extracted_parse(const char* mul_text, uint64_t mul_len, const char* add_text, uint64_t add_len,
+                           gkrgpu_parsed** out);
+int gkrgpu_parsed_layers(const gkrgpu_parsed* parsed);
+int gkrgpu_parsed_layer(const gkrgpu_parsed* parsed, int layer, gkrgpu_layer_desc* out);
+void gkrgpu_parsed_free(gkrgpu_parsed* parsed);
+
 /* Proof bytes of Prover::prove for this circuit: RAW commitment (2^nb_input_vars(0) rows
  * of 4N bytes) + 32 grinding bytes + per layer R*(6*nb_input_vars + 2) rows of 4N bytes. */
 uint64_t gkrgpu_proof_size(const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits);

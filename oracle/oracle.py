@@ -216,6 +216,34 @@ class Reference:
     def available():
         return os.path.exists(_build.REF_SO)
 
+    def _loaded_layers(self, n):
+        L = self.lib
+        L.ref_loaded_layer.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 6
+        out = []
+        for k in range(n):
+            nb_in, nb_out = ctypes.c_uint32(), ctypes.c_uint32()
+            nm, na = ctypes.c_uint64(), ctypes.c_uint64()
+            L.ref_loaded_layer(k, ctypes.byref(nb_in), ctypes.byref(nb_out), ctypes.byref(nm), ctypes.byref(na),
+                               None, None)
+            mul = np.empty((nm.value, 4), np.uint32)
+            add = np.empty((na.value, 3), np.uint32)
+            L.ref_loaded_layer(k, ctypes.byref(nb_in), ctypes.byref(nb_out), ctypes.byref(nm), ctypes.byref(na),
+                               mul.ctypes.data, add.ctypes.data)
+            out.append((nb_in.value, nb_out.value, mul, add))
+        return out
+
+    def circuit2_layers(self, data: bytes):
+        """[(nb_input_vars, nb_output_vars, mul, add)] of the reference's CircuitRaw reader +
+        Circuit::from_circuit_raw on a well-formed CIRCUIT2 file."""
+        self.lib.ref_circuit2_load.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        b = np.frombuffer(bytes(data), np.uint8)
+        return self._loaded_layers(self.lib.ref_circuit2_load(b.ctypes.data, b.size))
+
+    def extracted_layers(self, mul_path: str, add_path: str):
+        """The same through Circuit::load_extracted_gates on two text files."""
+        self.lib.ref_extracted_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        return self._loaded_layers(self.lib.ref_extracted_load(mul_path.encode(), add_path.encode()))
+
     def prove(self, circuit, witness, grinding_bits=10, native=False):
         w = np.ascontiguousarray(witness, dtype=np.uint32)
         N = w.shape[1]

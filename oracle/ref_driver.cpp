@@ -29,6 +29,8 @@
 #include <cstdio>
 #include <cstring>
 #include <fcntl.h>
+#include <sstream>
+#include <string>
 #include <unistd.h>
 
 #include "bn254.h"
@@ -322,6 +324,49 @@ void ref_bn254_reduce(const uint8_t* a, uint8_t* out) { bn_to_bytes(bn_from_byte
 void ref_sha256(const uint8_t* in, uint64_t len, uint8_t* out) {
     gkr::SHA256Hasher h;
     h.hash(out, in, (gkr::uint32)len);
+}
+
+// Circuit files through the reference's own loaders: CircuitRaw::operator>> and
+// Circuit::from_circuit_raw (CIRCUIT2), or Circuit::load_extracted_gates (text files).
+// The flattened layers stay in a static circuit read back with ref_loaded_layer.  Inputs
+// must be well formed (the reference exits the process on a bad magic number).
+static gkr::Circuit<refdrv::M31L<8>, refdrv::M31> g_loaded;
+
+int ref_circuit2_load(const uint8_t* bytes, uint64_t len) {
+    std::istringstream is(std::string((const char*)bytes, len), std::ios::binary);
+    CircuitRaw<refdrv::M31> raw;
+    is >> raw;
+    g_loaded = gkr::Circuit<refdrv::M31L<8>, refdrv::M31>::from_circuit_raw(raw);
+    return (int)g_loaded.layers.size();
+}
+int ref_extracted_load(const char* mul_path, const char* add_path) {
+    g_loaded = gkr::Circuit<refdrv::M31L<8>, refdrv::M31>::load_extracted_gates(mul_path, add_path);
+    return (int)g_loaded.layers.size();
+}
+// Sizes of layer l (counts, then the gates into mul: n_mul x {o, i0, i1, coef}, add:
+// n_add x {o, i0, coef} when those are non-null).
+void ref_loaded_layer(int l, uint32_t* nb_in, uint32_t* nb_out, uint64_t* n_mul, uint64_t* n_add, uint32_t* mul,
+                      uint32_t* add) {
+    const auto& L = g_loaded.layers[l];
+    *nb_in = L.nb_input_vars;
+    *nb_out = L.nb_output_vars;
+    *n_mul = L.mul.sparse_evals.size();
+    *n_add = L.add.sparse_evals.size();
+    if (mul)
+        for (size_t k = 0; k < L.mul.sparse_evals.size(); k++) {
+            const auto& g = L.mul.sparse_evals[k];
+            mul[4 * k] = g.o_id;
+            mul[4 * k + 1] = g.i_ids[0];
+            mul[4 * k + 2] = g.i_ids[1];
+            mul[4 * k + 3] = g.coef.x;
+        }
+    if (add)
+        for (size_t k = 0; k < L.add.sparse_evals.size(); k++) {
+            const auto& g = L.add.sparse_evals[k];
+            add[3 * k] = g.o_id;
+            add[3 * k + 1] = g.i_ids[0];
+            add[3 * k + 2] = g.coef.x;
+        }
 }
 
 }
