@@ -26,7 +26,7 @@ namespace gkrgpu {
 const char* const kKernelNames[K_NUM_KERNELS] = {"check_canonical", "evaluate", "eq_table", "gate_weights",
                                                  "hg_build_round0", "round_fold_lane", "round_fold_scalar",
                                                  "phase2_s_build", "weighted_row_sum", "hg_rebuild_round1",
-                                                 "bn254_load",
+                                                 "verifier_gate_sums", "canonicalize", "bn254_load",
                                                  "bn254_evaluate", "bn254_eq_table", "bn254_gate_weights",
                                                  "bn254_hg_build_round0", "bn254_round_fold_lane",
                                                  "bn254_round_fold_scalar", "bn254_phase2_s_build",
@@ -127,6 +127,69 @@ __global__ void k_check_canonical(const uint32_t* __restrict__ v, uint64_t n, un
         bad |= (x.x >= m31::P) | (x.y >= m31::P) | (x.z >= m31::P) | (x.w >= m31::P);
     }
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+}
+
+// In-place M31::from_bytes of u32 words (the verifier reads the commitment from proof bytes).
+__global__ void k_canonicalize(uint32_t* v, uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) v[i] = m31::from_u32(v[i]);
+}
+
+// ---------------------------------------------------------------- verifier gate sums
+// eval_sparse_circuit_connect_poly (include/LinearGKR/sumcheck_verifier_utils.hpp:22-56)
+// for R points at once: mul sums c * eqz_j[o] * eqx_j[i0] * eqy_j[i1] over the mul gates
+// (MUL), or add sums c * eqz_j[o] * eqx_j[i0] over the add gates, walked by output o (the
+// evaluate CSR).  Block partials go to 64-bit accumulators; the last block writes the R
+// canonical totals and re-zeroes the scratch.
+template <bool MUL>
+__global__ void __launch_bounds__(256) k_gate_sums(uint64_t O, uint64_t I, const uint32_t* __restrict__ off,
+                                                   const uint32_t* __restrict__ gates, const uint32_t* __restrict__ eqz,
+                                                   const uint32_t* __restrict__ eqx, const uint32_t* __restrict__ eqy,
+                                                   uint32_t reps, unsigned long long* acc, unsigned int* ticket,
+                                                   uint32_t* out) {
+    uint32_t s[3] = {0u, 0u, 0u};
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; o < O; o += stride) {
+        const uint32_t k0 = __ldg(off + o), k1 = __ldg(off + o + 1);
+        for (uint32_t k = k0; k < k1; k++) {
+            uint32_t i0, i1 = 0, c;
+            if (MUL) {
+                const uint4 g = __ldg(reinterpret_cast<const uint4*>(gates) + k);  // (i0, i1, c, 0)
+                i0 = g.x; i1 = g.y; c = g.z;
+            } else {
+                const uint2 g = __ldg(reinterpret_cast<const uint2*>(gates) + k);  // (i0, c)
+                i0 = g.x; c = g.y;
+            }
+            for (uint32_t j = 0; j < reps; j++) {
+                uint32_t t = mul(mul(c, __ldg(eqz + (uint64_t)j * O + o)), __ldg(eqx + (uint64_t)j * I + i0));
+                if (MUL) t = mul(t, __ldg(eqy + (uint64_t)j * I + i1));
+                s[j] = add(s[j], t);
+            }
+        }
+    }
+    __shared__ unsigned long long part[3];
+    if (threadIdx.x < 3) part[threadIdx.x] = 0ull;
+    __syncthreads();
+    for (uint32_t j = 0; j < reps; j++) {
+        unsigned long long x = s[j];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) x += __shfl_xor_sync(0xffffffffu, x, d);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&part[j], x);
+    }
+    __syncthreads();
+    if (threadIdx.x < reps) atomicAdd(&acc[threadIdx.x], part[threadIdx.x]);
+    __threadfence();
+    __syncthreads();
+    __shared__ unsigned int is_last;
+    if (threadIdx.x == 0) is_last = (atomicAdd(ticket, 1u) == gridDim.x - 1) ? 1u : 0u;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    if (threadIdx.x < reps) {
+        out[threadIdx.x] = reduce64(__ldcg(&acc[threadIdx.x]));
+        acc[threadIdx.x] = 0ull;
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
 }
 
 // ---------------------------------------------------------------- layer evaluation
@@ -604,6 +667,21 @@ cudaError_t launch_evaluate(const uint32_t* in, uint32_t* out, uint64_t O, const
     return cudaGetLastError();
 }
 
+cudaError_t launch_canonicalize(uint32_t* v, uint64_t n, cudaStream_t s) {
+    k_canonicalize<<<grid_1d(n, 256), 256, 0, s>>>(v, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_gate_sums(bool mul_gates, uint64_t O, uint64_t I, const uint32_t* off, const uint32_t* gates,
+                             const uint32_t* eqz, const uint32_t* eqx, const uint32_t* eqy, uint32_t reps,
+                             unsigned long long* acc, unsigned int* ticket, uint32_t* out, cudaStream_t s) {
+    if (reps < 1 || reps > 3) return cudaErrorInvalidValue;
+    const uint32_t grid = grid_1d(O, 256);
+    if (mul_gates)
+        k_gate_sums<true><<<grid, 256, 0, s>>>(O, I, off, gates, eqz, eqx, eqy, reps, acc, ticket, out);
+    else
+        k_gate_sums<false><<<grid, 256, 0, s>>>(O, I, off, gates, eqz, eqx, eqy, reps, acc, ticket, out);
+    return cudaGetLastError();
+}
 cudaError_t launch_eq(uint32_t* out, const EqArgs& a, cudaStream_t s) {
     k_eq<<<grid_1d(1ull << a.nvars, 256), 256, 0, s>>>(out, a);
     return cudaGetLastError();

@@ -58,6 +58,8 @@ enum KernelId {
     K_S_BUILD,
     K_WSUM,
     K_HG_ROUND1,
+    K_GATE_SUMS,   // verifier
+    K_CANONICAL,   // verifier
     // BN254 kernels (bn254.cuh)
     K_BN_LOAD,
     K_BN_EVALUATE,
@@ -78,6 +80,15 @@ LaunchShape row_shape(const Geo& g, uint64_t rows, uint32_t block, uint32_t ctas
 
 // Launch wrappers (all asynchronous on `s`).
 cudaError_t launch_check_canonical(const uint32_t* v, uint64_t n, unsigned int* flag, cudaStream_t s);
+// v[i] = v[i] mod p in place (M31::from_bytes of raw proof words).
+cudaError_t launch_canonicalize(uint32_t* v, uint64_t n, cudaStream_t s);
+// Verifier gate sums for `reps` points: over the mul gates (CSR by output: off, (i0, i1, c, 0)
+// gates) sum c eqz_j[o] eqx_j[i0] eqy_j[i1], or over the add gates ((i0, c) gates) sum
+// c eqz_j[o] eqx_j[i0]; eq tables are reps x O / reps x I.  acc (3 x u64) and ticket must be
+// zero and are left zero; out receives reps canonical totals.
+cudaError_t launch_gate_sums(bool mul_gates, uint64_t O, uint64_t I, const uint32_t* off, const uint32_t* gates,
+                             const uint32_t* eqz, const uint32_t* eqx, const uint32_t* eqy, uint32_t reps,
+                             unsigned long long* acc, unsigned int* ticket, uint32_t* out, cudaStream_t s);
 cudaError_t launch_evaluate(const uint32_t* in, uint32_t* out, uint64_t O, const uint32_t* mo_off, const uint4* mo_g,
                             const uint32_t* ao_off, const uint2* ao_g, const Geo& g, uint32_t block, uint32_t ctas,
                             cudaStream_t s);

@@ -996,6 +996,7 @@ struct Prover {
 };
 
 #include "bn254_prover.cuh"
+#include "verifier.cuh"
 
 void check_ctx(gkrgpu_ctx* ctx) {
     if (!ctx) fail(GKRGPU_ERR_INVALID, "null context");
@@ -1461,6 +1462,25 @@ int gkrgpu_prove_device(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
     }
     return prove_entry(ctx, circuit, n_copies, grinding_bits, nullptr, d_input, proof_out, proof_cap, proof_len,
                        claimed_v);
+}
+
+int gkrgpu_verify(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
+                  const uint8_t* proof, uint64_t proof_len, const uint32_t* claimed_v, int* accepted) {
+    return guarded([&] {
+        check_run(ctx, circuit, n_copies);
+        if (!proof || !claimed_v || !accepted) fail(GKRGPU_ERR_INVALID, "null buffer");
+        *accepted = 0;
+        if (circuit->field != GKRGPU_FIELD_M31) fail(GKRGPU_ERR_INVALID, "the verifier supports M31 circuits");
+        if (grinding_bits < 0 || grinding_bits > 30) fail(GKRGPU_ERR_INVALID, "grinding_bits must be in [0, 30]");
+        const int R = reps_for(grinding_bits);
+        if (R < 1 || R > 3) fail(GKRGPU_ERR_INVALID, "grinding_bits %d gives %d repetitions (1..3 supported)", grinding_bits, R);
+        for (const auto& l : circuit->layers)
+            if (l.nin > 32 || l.nout > 32) fail(GKRGPU_ERR_INVALID, "layer too wide");
+        on_idle_lane(ctx, [&](Lane& lane) {
+            Verifier v(*ctx, lane, *circuit, n_copies, R);
+            *accepted = v.run(grinding_bits, proof, proof_len, claimed_v) ? 1 : 0;
+        });
+    });
 }
 
 int gkrgpu_eval_multilinear(gkrgpu_ctx* ctx, const uint32_t* d_evals, uint32_t nb_vars, uint32_t n_copies,

@@ -70,6 +70,7 @@ SIGNATURES = [
     ("gkrgpu_prove_device", _I, [_P, _P, _U32, _I, _P, _P, _U64, ctypes.POINTER(_U64), _P]),
     ("gkrgpu_prove_submit", _I, [_P, _P, _U32, _I, _P, _I, _P, _U64, _P, _I, ctypes.POINTER(_P)]),
     ("gkrgpu_prove_wait", _I, [_P, ctypes.POINTER(_U64)]),
+    ("gkrgpu_verify", _I, [_P, _P, _U32, _I, _P, _U64, _P, ctypes.POINTER(_I)]),
     ("gkrgpu_set_concurrency", _I, [_P, _I, _U64]),
     ("gkrgpu_workspace_bytes", _U64, [_P, _U32, _I, _I]),
     ("gkrgpu_memory_stats", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),

@@ -202,6 +202,17 @@ class Context:
         _lib.check(_lib.load().gkrgpu_prove_wait(h, ctypes.byref(plen)))
         return plen.value
 
+    def verify(self, dc: DeviceCircuit, proof, claimed_v, grinding_bits=10) -> bool:
+        """Verifier::verify of an M31 proof (gkrgpu_verify): True when the reference verifier
+        accepts.  claimed_v is the (R, N) uint32 table the prover returned."""
+        cv = _table(dc.field, claimed_v)
+        pb = np.frombuffer(bytes(proof), np.uint8)
+        ok = ctypes.c_int()
+        _lib.check(_lib.load().gkrgpu_verify(self.handle, dc.handle, cv.shape[1], grinding_bits,
+                                             pb.ctypes.data if pb.size else None, pb.size, cv.ctypes.data,
+                                             ctypes.byref(ok)))
+        return ok.value == 1
+
     def eval_multilinear(self, d_evals: int, nb_vars: int, n_copies: int, points):
         """eval_multilinear of the device table at d_evals (2^nb_vars rows) at 1..3 points;
         returns (n_points, n_copies) uint32."""
@@ -346,3 +357,21 @@ class Prover:
             raise ValueError("no circuit input: call circuit.set_input(values) or pass witness")
         cv, proof = self.ctx.prove(self._dc, w, self.config.grinding_bits)
         return cv, Proof(proof)
+
+
+class Verifier:
+    """gkr::Verifier (include/LinearGKR/LinearGKR.hpp:92-149) with its device-side parts on the
+    GPU (gkrgpu_verify); M31 circuits."""
+
+    def __init__(self, config: Config = None, ctx: Context = None):
+        self.config = config or Config()
+        self.ctx = ctx or Context(0)
+        self._dc = None
+        self._circuit = None
+
+    def verify(self, circuit: Circuit, claimed_v, proof) -> bool:
+        if self._circuit is not circuit:
+            self._dc = self.ctx.load(circuit, self.config.field_type)
+            self._circuit = circuit
+        data = proof.bytes if isinstance(proof, Proof) else proof
+        return self.ctx.verify(self._dc, data, claimed_v, self.config.grinding_bits)

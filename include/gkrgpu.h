@@ -153,6 +153,17 @@ int gkrgpu_prove_device(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
                         const uint32_t* d_input, uint8_t* proof_out, uint64_t proof_cap, uint64_t* proof_len,
                         uint32_t* claimed_v);
 
+/* Verifier::verify (include/LinearGKR/LinearGKR.hpp:105-149: gkr_verify, gkr.hpp:75-122, and
+ * RawPC::verify, raw.hpp:75-78) of an M31 proof, GPU-assisted: the host replays the
+ * transcript and checks every round; the device computes each layer's
+ * eval_sparse_circuit_connect_poly (eq tables and gate sums,
+ * sumcheck_verifier_utils.hpp:22-56) and the multilinear evaluations of the committed input
+ * (the proof's first 2^nb_input_vars(0) rows).  claimed_v: R rows of n_copies lanes.
+ * *accepted is 1 when the reference verifier would accept, else 0 (the status is
+ * GKRGPU_OK either way; errors are bad arguments or device failures). */
+int gkrgpu_verify(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
+                  const uint8_t* proof, uint64_t proof_len, const uint32_t* claimed_v, int* accepted);
+
 /* Pipelined Prover::prove.  gkrgpu_prove_submit queues one proof and returns at once; its
  * host stage (RAW commitment bytes, their SHA-256, grinding) runs on a host worker while
  * earlier proofs' device stages run on the GPU, and device stages run one at a time in
