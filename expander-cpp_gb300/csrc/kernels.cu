@@ -26,7 +26,7 @@ namespace gkrgpu {
 const char* const kKernelNames[K_NUM_KERNELS] = {"check_canonical", "evaluate", "eq_table", "gate_weights",
                                                  "hg_build_round0", "round_fold_lane", "round_fold_scalar",
                                                  "phase2_s_build", "weighted_row_sum", "hg_rebuild_round1",
-                                                 "verifier_gate_sums", "canonicalize", "bn254_load",
+                                                 "verifier_gate_sums", "canonicalize", "phase2_round0", "bn254_load",
                                                  "bn254_evaluate", "bn254_eq_table", "bn254_gate_weights",
                                                  "bn254_hg_build_round0", "bn254_round_fold_lane",
                                                  "bn254_round_fold_scalar", "bn254_phase2_s_build",
@@ -578,6 +578,52 @@ __global__ void __launch_bounds__(256) k_round_shared(RoundPtrs p, uint64_t npai
     reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, LANE_HG ? nullptr : vx, g.N, (uint32_t)R});
 }
 
+// Phase-two round 0 (no fold): p0_j = sum f(2i) s_j(2i), p1_j = sum f(2i+1) s_j(2i+1),
+// p2raw_j = sum (f(2i) + f(2i+1)) (s_j(2i) + s_j(2i+1)) over the layer input f = v.  Three
+// products per pair, repetition and lane against 32 bytes read make this round bound by
+// integer instructions rather than HBM, so: one repetition per CTA (j = blockIdx.x % R,
+// the R CTAs of a row chunk adjacent so the rows come from L2 after the first read) for
+// light threads and high occupancy, and products summed unreduced in 64-bit accumulators,
+// folded mod p every third pair instead of fully reduced one by one.  Same results as
+// k_round_shared<R, false, false>.
+__global__ void __launch_bounds__(256) k_p2_round0(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx,
+                                                   Geo g, uint32_t reps, RedScratch red, uint32_t* evals_out) {
+    const TileIdx t = tile_idx(g);
+    const uint32_t j = blockIdx.x % reps, cx = blockIdx.x / reps, nx = gridDim.x / reps;
+    const uint32_t* __restrict__ fs = p.fsrc[0];
+    const uint2* __restrict__ sj =
+        reinterpret_cast<const uint2*>(j == 0 ? p.hsrc[0] : (j == 1 ? p.hsrc[1] : p.hsrc[2]));
+    uint64_t acc[3][4] = {};
+    if (t.active) {
+        uint32_t since_fold = 0;
+        for (uint64_t i = (uint64_t)cx * g.rps + t.rs; i < npairs; i += (uint64_t)nx * g.rps) {
+            const uint4 a0 = ld4(fs, 2 * i, g.N, t.lane0), a1 = ld4(fs, 2 * i + 1, g.N, t.lane0);
+            const uint2 s = __ldg(sj + i);
+            const uint32_t s01 = add(s.x, s.y);
+#pragma unroll
+            for (int l = 0; l < 4; l++) {
+                acc[0][l] += (uint64_t)comp(a0, l) * s.x;
+                acc[1][l] += (uint64_t)comp(a1, l) * s.y;
+                acc[2][l] += (uint64_t)add(comp(a0, l), comp(a1, l)) * s01;
+            }
+            // each product is < 2^62: after a fold (< 2^34) three more keep the sum < 2^64
+            if (++since_fold == 3) {
+                since_fold = 0;
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+#pragma unroll
+                    for (int l = 0; l < 4; l++) acc[c][l] = (acc[c][l] & m31::P) + (acc[c][l] >> 31);
+            }
+        }
+    }
+    uint32_t out[3][4];
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) out[c][l] = reduce64(acc[c][l]);
+    reduce_group<3>(out, g, t.active, red, 3 * j, RoundFin{red, evals_out, vx, g.N, reps});
+}
+
 // ---------------------------------------------------------------- phase two: s(y)
 // s_j[y] = sum over mul gates (z, x, y, c) of eqc_j[z] * eq_rx_j[x] * c: the
 // copy-independent factor of h(y) = v(rx) s(y) (sumcheck_helper.hpp:250-259).
@@ -726,14 +772,19 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, co
     if (reps < 1 || reps > 3) return cudaErrorInvalidValue;
     if (lane_hg && !fold_) return cudaErrorInvalidValue;  // phase-one round 0 lives in k_hg_round0
     if (!fold_ && !shared_src) return cudaErrorInvalidValue;
+    if (!fold_) {
+        // phase-two round 0: integer-bound, one repetition per CTA (k_p2_round0)
+        LaunchShape sh = rep_shape(g, npairs, block, ctas, reps);
+        k_p2_round0<<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, (uint32_t)reps, red, evals_out);
+        return cudaGetLastError();
+    }
     if (shared_src) {
         // one read of the shared layer input for all repetitions
         LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
 #define GKR_SHARED(RR, LH, FO) k_round_shared<RR, LH, FO><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out)
 #define GKR_SHARED_R(RR)                                  \
     if (lane_hg) GKR_SHARED(RR, true, true);              \
-    else if (fold_) GKR_SHARED(RR, false, true);          \
-    else GKR_SHARED(RR, false, false);
+    else GKR_SHARED(RR, false, true);
         switch (reps) {
             case 1: GKR_SHARED_R(1) break;
             case 2: GKR_SHARED_R(2) break;
@@ -748,11 +799,9 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, co
     if (lane_hg) {
         if (shared_src) GKR_ROUND(true, true, true);
         else GKR_ROUND(false, true, true);
-    } else if (fold_) {
+    } else {
         if (shared_src) GKR_ROUND(true, false, true);
         else GKR_ROUND(false, false, true);
-    } else {
-        GKR_ROUND(true, false, false);
     }
 #undef GKR_ROUND
     return cudaGetLastError();

@@ -60,6 +60,7 @@ enum KernelId {
     K_HG_ROUND1,
     K_GATE_SUMS,   // verifier
     K_CANONICAL,   // verifier
+    K_P2_ROUND0,
     // BN254 kernels (bn254.cuh)
     K_BN_LOAD,
     K_BN_EVALUATE,

@@ -888,11 +888,11 @@ struct Prover {
             p.fsrc[0] = v;
             for (int j = 0; j < R; j++) p.hsrc[j] = ws.sb[0] + j * sstride;
             const uint64_t npairs = I >> 1;
-            c.launch(K_ROUND_SCALAR, rb * 2.0 * npairs + 8.0 * R * npairs, [&] {
-                return launch_round(R, true, false, false, p, npairs, ws.vx, gk[K_ROUND_SCALAR], X.block,
-                                    ck_ctas[K_ROUND_SCALAR], red_mapped(), c.evals_d(), c.stream);
+            c.launch(K_P2_ROUND0, rb * 2.0 * npairs + 8.0 * R * npairs, [&] {
+                return launch_round(R, true, false, false, p, npairs, ws.vx, gk[K_P2_ROUND0], X.block,
+                                    ck_ctas[K_P2_ROUND0], red_mapped(), c.evals_d(), c.stream);
             });
-            fetch(groups(K_ROUND_SCALAR), n == 1 ? vsrc : nullptr, true);
+            fetch(groups(K_P2_ROUND0), n == 1 ? vsrc : nullptr, true);
             transcript_round(t, ry, 0, n == 1, false, vy.data());
         }
         for (int j = 0; j < R; j++) cur_f[j] = v;
@@ -1707,7 +1707,8 @@ int gkrgpu_autotune(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_c
         };
         const std::vector<int> kinds =
             bn ? std::vector<int>{K_BN_EVALUATE, K_BN_HG_ROUND0, K_BN_ROUND_LANE, K_BN_ROUND_SCALAR, K_BN_WSUM}
-               : std::vector<int>{K_EVALUATE, K_HG_ROUND0, K_HG_ROUND1, K_ROUND_LANE, K_ROUND_SCALAR, K_WSUM};
+               : std::vector<int>{K_EVALUATE, K_HG_ROUND0, K_HG_ROUND1, K_ROUND_LANE, K_ROUND_SCALAR, K_P2_ROUND0,
+                                  K_WSUM};
         try {
             double ms[K_NUM_KERNELS];
             run(ms);  // warm-up: pool growth, first-launch costs
