@@ -396,17 +396,90 @@ __device__ __forceinline__ void accum(Fr (&acc)[3], const Fr& f0, const Fr& f1, 
 }
 
 // ---------------------------------------------------------------- kernels
-// Canonical input -> Montgomery table; an element >= r raises *bad (and is stored as 0).
+// Input -> Montgomery table.  Canonical input (bad != null): an element >= r raises *bad
+// and is stored as 0.  Otherwise every element is first reduced mod r (from_bytes of
+// arbitrary 32-byte words: 2^256 < 6r, so at most five subtractions).
 __global__ void k_load(const uint32_t* __restrict__ canon, uint32_t* __restrict__ mont, uint64_t n, unsigned int* bad) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         Fr x = lds(reinterpret_cast<const Fr*>(canon), i);
         uint32_t d[8];
-        if (minus_r(x.l, d) == 0u) {  // no borrow: x >= r
-            atomicOr(bad, 1u);
-            x = zero();
+        if (bad) {
+            if (minus_r(x.l, d) == 0u) {  // no borrow: x >= r
+                atomicOr(bad, 1u);
+                x = zero();
+            }
+        } else {
+            for (int k = 0; k < 5 && minus_r(x.l, d) == 0u; k++)
+#pragma unroll
+                for (int q = 0; q < 8; q++) x.l[q] = d[q];
         }
         sts(reinterpret_cast<Fr*>(mont), i, to_mont(x));
+    }
+}
+
+// Verifier gate sums (eval_sparse_circuit_connect_poly, one repetition): over the mul gates
+// sum c eqz[o] eqx[i0] eqy[i1], or over the add gates sum c eqz[o] eqx[i0], walked by output
+// (the evaluate CSR with Montgomery coefficients).  Thread sums -> warp shuffles -> shared
+// memory -> 64-bit limb sums; the last block writes the canonical total (one REDC).
+template <bool MUL>
+__global__ void __launch_bounds__(256) k_gate_sums(uint64_t O, const uint32_t* __restrict__ off,
+                                                   const uint32_t* __restrict__ gates, const Fr* __restrict__ coef,
+                                                   const Fr* __restrict__ eqz, const Fr* __restrict__ eqx,
+                                                   const Fr* __restrict__ eqy, unsigned long long* acc,
+                                                   unsigned int* ticket, uint32_t* out) {
+    Fr s = zero();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; o < O; o += stride) {
+        const uint32_t k0 = __ldg(off + o), k1 = __ldg(off + o + 1);
+        if (k0 == k1) continue;
+        const Fr ez = lds(eqz, o);
+        for (uint32_t k = k0; k < k1; k++) {
+            Fr t;
+            if (MUL) {
+                const uint4 g = __ldg(reinterpret_cast<const uint4*>(gates) + k);  // (i0, i1, c, 0)
+                t = mul(mul(lds(eqx, g.x), lds(eqy, g.y)), lds(coef, k));
+            } else {
+                const uint2 g = __ldg(reinterpret_cast<const uint2*>(gates) + k);  // (i0, c)
+                t = mul(lds(eqx, g.x), lds(coef, k));
+            }
+            s = add(s, mul(t, ez));
+        }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        Fr o;
+#pragma unroll
+        for (int k = 0; k < 8; k++) o.l[k] = __shfl_xor_sync(0xffffffffu, s.l[k], d);
+        s = add(s, o);
+    }
+    __shared__ Fr part[8];
+    const uint32_t w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0) part[w] = s;
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        unsigned long long limb = 0;
+        for (uint32_t q = 0; q < nw; q++) limb += part[q].l[threadIdx.x];
+        atomicAdd(&acc[threadIdx.x], limb);
+    }
+    __threadfence();
+    __syncthreads();
+    __shared__ unsigned int is_last;
+    if (threadIdx.x == 0) is_last = (atomicAdd(ticket, 1u) == gridDim.x - 1) ? 1u : 0u;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    if (threadIdx.x == 0) {
+        unsigned long long t[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            t[k] = __ldcg(acc + k);
+            acc[k] = 0ull;
+        }
+        const Fr r = redc_sums(t);
+#pragma unroll
+        for (int k = 0; k < 8; k++) out[k] = r.l[k];
+        *ticket = 0u;
     }
 }
 
@@ -649,6 +722,17 @@ dim3 grid_rows(const GeoBn& g, uint64_t rows, uint32_t ctas) {
 
 cudaError_t launch_load(const uint32_t* canon, uint32_t* mont, uint64_t n_elems, unsigned int* bad, cudaStream_t s) {
     k_load<<<grid1(n_elems), 256, 0, s>>>(canon, mont, n_elems, bad);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gate_sums(bool mul_gates, uint64_t O, const uint32_t* off, const uint32_t* gates, const Fr* coef,
+                             const Fr* eqz, const Fr* eqx, const Fr* eqy, unsigned long long* acc,
+                             unsigned int* ticket, uint32_t* out, cudaStream_t s) {
+    const uint32_t grid = grid1(O);
+    if (mul_gates)
+        k_gate_sums<true><<<grid, kBlock, 0, s>>>(O, off, gates, coef, eqz, eqx, eqy, acc, ticket, out);
+    else
+        k_gate_sums<false><<<grid, kBlock, 0, s>>>(O, off, gates, coef, eqz, eqx, eqy, acc, ticket, out);
     return cudaGetLastError();
 }
 

@@ -49,7 +49,15 @@ struct RoundPtrsBn {
     uint32_t r[8];  // challenge of the previous round, Montgomery form
 };
 
+// Input -> Montgomery table; with bad a non-canonical element raises *bad, without it every
+// element is reduced mod r first (the verifier's from_bytes).
 cudaError_t launch_load(const uint32_t* canon, uint32_t* mont, uint64_t n_elems, unsigned int* bad, cudaStream_t s);
+// Verifier gate sums of one layer (one repetition): mul or add gates of the evaluate CSR with
+// their Montgomery coefficients; acc (8 x u64) and ticket zero before and after; out receives
+// the canonical total (8 words).
+cudaError_t launch_gate_sums(bool mul_gates, uint64_t O, const uint32_t* off, const uint32_t* gates, const Fr* coef,
+                             const Fr* eqz, const Fr* eqx, const Fr* eqy, unsigned long long* acc,
+                             unsigned int* ticket, uint32_t* out, cudaStream_t s);
 cudaError_t launch_unload(uint32_t* v, uint64_t n_elems, cudaStream_t s);
 cudaError_t launch_evaluate(const uint32_t* in, uint32_t* out, uint64_t O, const uint32_t* mo_off, const uint4* mo_g,
                             const Fr* mo_c, const uint32_t* ao_off, const uint2* ao_g, const Fr* ao_c, const GeoBn& g,

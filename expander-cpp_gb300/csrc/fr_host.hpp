@@ -102,6 +102,11 @@ inline Fr mont(const Fr& a, const Fr& b) {
     return r;
 }
 inline Fr to_mont(const Fr& a) { return mont(a, Fr{{kR2[0], kR2[1], kR2[2], kR2[3]}}); }
+// a * b mod r of canonical values (two Montgomery products)
+inline Fr mul(const Fr& a, const Fr& b) { return to_mont(mont(a, b)); }
+// (r + 1) / 2, the inverse of 2
+constexpr uint64_t kInv2[4] = {0xa1f0fac9f8000001ull, 0x9419f4243cdcb848ull, 0xdc2822db40c0ac2eull,
+                               0x183227397098d014ull};
 inline Fr from_mont(const Fr& a) { return mont(a, Fr{{1, 0, 0, 0}}); }
 // f0 + r (f1 - f0), all in the same (Montgomery) form.
 inline Fr fold_mont(const Fr& f0, const Fr& f1, const Fr& r_mont) { return add(f0, mont(sub(f1, f0), r_mont)); }

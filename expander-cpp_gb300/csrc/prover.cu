@@ -1470,15 +1470,17 @@ int gkrgpu_verify(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_cop
         check_run(ctx, circuit, n_copies);
         if (!proof || !claimed_v || !accepted) fail(GKRGPU_ERR_INVALID, "null buffer");
         *accepted = 0;
-        if (circuit->field != GKRGPU_FIELD_M31) fail(GKRGPU_ERR_INVALID, "the verifier supports M31 circuits");
         if (grinding_bits < 0 || grinding_bits > 30) fail(GKRGPU_ERR_INVALID, "grinding_bits must be in [0, 30]");
-        const int R = reps_for(grinding_bits);
+        const int R = reps_for_field(circuit->field, grinding_bits);
         if (R < 1 || R > 3) fail(GKRGPU_ERR_INVALID, "grinding_bits %d gives %d repetitions (1..3 supported)", grinding_bits, R);
-        for (const auto& l : circuit->layers)
-            if (l.nin > 32 || l.nout > 32) fail(GKRGPU_ERR_INVALID, "layer too wide");
         on_idle_lane(ctx, [&](Lane& lane) {
-            Verifier v(*ctx, lane, *circuit, n_copies, R);
-            *accepted = v.run(grinding_bits, proof, proof_len, claimed_v) ? 1 : 0;
+            if (circuit->field == GKRGPU_FIELD_BN254) {
+                BnVerifier v(*ctx, lane, *circuit, n_copies);
+                *accepted = v.run(grinding_bits, proof, proof_len, claimed_v) ? 1 : 0;
+            } else {
+                Verifier v(*ctx, lane, *circuit, n_copies, R);
+                *accepted = v.run(grinding_bits, proof, proof_len, claimed_v) ? 1 : 0;
+            }
         });
     });
 }

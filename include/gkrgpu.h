@@ -1,4 +1,4 @@
-/* gkrgpu: GB300-native GKR prover for data-parallel layered circuits over M31.
+/* gkrgpu: GB300-native GKR prover for data-parallel layered circuits over M31 and BN254.
  *
  * C ABI of the drop-in boundary.  Each entry point replaces one piece of the reference
  * prove path of PolyhedraZK/Expander-cpp (file:line below are paths in that project).
@@ -154,7 +154,7 @@ int gkrgpu_prove_device(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
                         uint32_t* claimed_v);
 
 /* Verifier::verify (include/LinearGKR/LinearGKR.hpp:105-149: gkr_verify, gkr.hpp:75-122, and
- * RawPC::verify, raw.hpp:75-78) of an M31 proof, GPU-assisted: the host replays the
+ * RawPC::verify, raw.hpp:75-78), GPU-assisted, for M31 and BN254 circuits: the host replays the
  * transcript and checks every round; the device computes each layer's
  * eval_sparse_circuit_connect_poly (eq tables and gate sums,
  * sumcheck_verifier_utils.hpp:22-56) and the multilinear evaluations of the committed input

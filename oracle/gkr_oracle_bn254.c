@@ -499,7 +499,7 @@ int oracle_bn254_verify(const oracle_layer* L, int nl, uint32_t N, const uint64_
     eval_ml(commitment, n0, N, rz2, e);
     for (uint32_t k = 0; k < N; k++)
         if (!fe_eq(e[k], cv2[k])) verified = 0;
-    if (pr.bad || pr.idx != proof_len) verified = 0;
+    if (pr.bad) verified = 0; /* like the reference, bytes after the last claim are not read */
     free(e);
     free(commitment);
     free(tbuf);

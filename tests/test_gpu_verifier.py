@@ -77,10 +77,30 @@ def test_verifier_on_larger_circuits(ctx, oracle, seed, widths, n):
     assert not oracle.verify(circ, w, bad, proof)
 
 
-def test_verifier_rejects_bn254_circuits(ctx):
-    from gkr_gb300._lib import GkrGpuError
-    circ, w, g = cases.build_bn("bn_width_one_n4")
+@pytest.mark.parametrize("name", ["bn_mixed_widths_n16", "bn_width_one_n4", "bn_full_coefs_n8", "bn_lanes64",
+                                  "bn_grind0_n8"])
+def test_bn254_verifier_decisions_match_oracle(ctx, name):
+    from oracle.oracle import OracleBn254
+    obn = OracleBn254()
+    circ, w, g = cases.build_bn(name)
     dc = ctx.load(circ, "BN254")
     cv, proof = ctx.prove(dc, w, grinding_bits=g)
-    with pytest.raises(GkrGpuError):
-        ctx.verify(dc, proof, cv, grinding_bits=g)
+    N = w.shape[1]
+    com = (1 << circ.log_input_size) * N * 32
+    bad_cv = cv.copy()
+    bad_cv[0, N - 1, 0] ^= np.uint64(2)
+    variants = {
+        "honest": (proof, cv),
+        "commitment": (_flip(proof, 33), cv),
+        "first round": (_flip(proof, com + 32 + 40), cv),
+        "last vy": (_flip(proof, len(proof) - 5), cv),
+        "truncated": (proof[:-32], cv),
+        "claim": (proof, bad_cv),
+        "grinding bytes": (_flip(proof, com + 9), cv),
+        "trailing bytes": (proof + bytes(8), cv),
+    }
+    for what, (pb, c) in variants.items():
+        want = obn.verify(circ, w, c, pb, grinding_bits=g)
+        assert ctx.verify(dc, pb, c, grinding_bits=g) == want, what
+    assert ctx.verify(dc, proof, cv, grinding_bits=g)
+    assert not ctx.verify(dc, proof, bad_cv, grinding_bits=g)
