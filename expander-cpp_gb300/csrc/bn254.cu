@@ -285,8 +285,21 @@ __device__ __forceinline__ Tile tile(const GeoBn& g) {
     return t;
 }
 
+// Canonical total of component c of one lane; leaves its accumulators zeroed.
+__device__ __forceinline__ Fr take(const RedBn& red, uint32_t c, uint32_t N, uint32_t lane) {
+    unsigned long long s[8];
+    unsigned long long* p = &red.acc[((size_t)c * N + lane) * 8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        s[k] = __ldcg(p + k);
+        p[k] = 0ull;
+    }
+    return redc_sums(s);
+}
+
 // C components per thread -> shared-memory sum over the CTA's row slices -> 64-bit
-// atomic adds per limb -> the last CTA of the lane group hands its lanes to fin(lane).
+// atomic adds per limb -> the last CTA of the lane group finishes its lanes: one thread per
+// (component, lane) total, then fin(c, lane, totals of the lane, tpr) per output value.
 template <int C, class Fin>
 __device__ __forceinline__ void reduce_bn(Fr (&acc)[C], const GeoBn& g, bool active, RedBn red, Fin fin) {
     extern __shared__ uint32_t smem[];
@@ -336,7 +349,18 @@ __device__ __forceinline__ void reduce_bn(Fr (&acc)[C], const GeoBn& g, bool act
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    for (uint32_t li = tid; li < g.tpr; li += B) fin(blockIdx.y * g.tpr + li);
+    // the last CTA: every (component, lane) total is reduced by its own thread, then each
+    // output value is finished by its own thread (the finisher's chains run in parallel)
+    Fr* tot = reinterpret_cast<Fr*>(smem);
+    for (uint32_t o = tid; o < (uint32_t)C * g.tpr; o += B) {
+        const uint32_t c = o / g.tpr, li = o - c * g.tpr;
+        tot[o] = take(red, c, g.N, blockIdx.y * g.tpr + li);
+    }
+    __syncthreads();
+    for (uint32_t o = tid; o < (uint32_t)C * g.tpr; o += B) {
+        const uint32_t c = o / g.tpr, li = o - c * g.tpr;
+        fin(c, blockIdx.y * g.tpr + li, tot + li, g.tpr);
+    }
     if (tid == 0) red.ticket[blockIdx.y] = 0u;
     if (red.done) {
         __threadfence_system();
@@ -345,48 +369,34 @@ __device__ __forceinline__ void reduce_bn(Fr (&acc)[C], const GeoBn& g, bool act
     }
 }
 
-// Canonical total of component c of one lane; leaves its accumulators zeroed.
-__device__ __forceinline__ Fr take(const RedBn& red, uint32_t c, uint32_t N, uint32_t lane) {
-    unsigned long long s[8];
-    unsigned long long* p = &red.acc[((size_t)c * N + lane) * 8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        s[k] = __ldcg(p + k);
-        p[k] = 0ull;
-    }
-    return redc_sums(s);
-}
-
-// Evaluations at 0, 1, 2 (canonical) of one lane; phase two multiplies by vx: a Montgomery
-// product of a canonical value with vx's Montgomery form is the canonical product.
+// Output c of one lane from the canonical totals t[0], t[tpr], t[2 tpr] (components 0..2 of
+// that lane): the evaluations at 0, 1 and 2 (6 p1 + 3 p0 - 2 p2raw).  Phase two multiplies
+// by vx: a Montgomery product of a canonical value with vx's Montgomery form is the
+// canonical product.
 struct RoundFinBn {
-    RedBn red;
     uint32_t* out;  // 3 x N x 8 limbs, canonical
     const uint32_t* vx;
     uint32_t N;
-    __device__ void operator()(uint32_t lane) const {
-        Fr p0 = take(red, 0, N, lane), p1 = take(red, 1, N, lane), p2r = take(red, 2, N, lane);
-        const Fr p1x2 = add(p1, p1);
-        Fr p2 = add(add(p1x2, p1x2), p1x2);             // 6 p1
-        p2 = add(p2, add(add(p0, p0), p0));            // + 3 p0
-        p2 = sub(p2, add(p2r, p2r));                    // - 2 p2raw
-        if (vx) {
-            const Fr x = ldf(vx, 0, N, lane);
-            p0 = mul(p0, x);
-            p1 = mul(p1, x);
-            p2 = mul(p2, x);
+    __device__ void operator()(uint32_t c, uint32_t lane, const Fr* t, uint32_t tpr) const {
+        Fr v;
+        if (c < 2) {
+            v = t[c * tpr];
+        } else {
+            const Fr p0 = t[0], p1 = t[tpr], p2r = t[2 * tpr];
+            const Fr p1x2 = add(p1, p1);
+            v = add(add(p1x2, p1x2), p1x2);       // 6 p1
+            v = add(v, add(add(p0, p0), p0));    // + 3 p0
+            v = sub(v, add(p2r, p2r));            // - 2 p2raw
         }
-        stf(out, 0, N, lane, p0);
-        stf(out, 1, N, lane, p1);
-        stf(out, 2, N, lane, p2);
+        if (vx) v = mul(v, ldf(vx, 0, N, lane));
+        stf(out, c, N, lane, v);
     }
 };
 
 struct CopyFinBn {
-    RedBn red;
     uint32_t* out;  // N x 8 limbs, canonical
     uint32_t N;
-    __device__ void operator()(uint32_t lane) const { stf(out, 0, N, lane, take(red, 0, N, lane)); }
+    __device__ void operator()(uint32_t, uint32_t lane, const Fr* t, uint32_t) const { stf(out, 0, N, lane, t[0]); }
 };
 
 __device__ __forceinline__ void accum(Fr (&acc)[3], const Fr& f0, const Fr& f1, const Fr& h0, const Fr& h1) {
@@ -607,7 +617,7 @@ __global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ 
             accum(acc, ldf(v, 2 * i, g.N, t.q), ldf(v, 2 * i + 1, g.N, t.q), h[0], h[1]);
         }
     }
-    reduce_bn<3>(acc, g, t.active, red, RoundFinBn{red, evals_out, nullptr, g.N});
+    reduce_bn<3>(acc, g, t.active, red, RoundFinBn{evals_out, nullptr, g.N});
 }
 
 template <bool LANE_HG, bool FOLD>
@@ -674,7 +684,7 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrsBn p, uint64_t npairs, c
         }
         if (valid) accum(acc, f0, f1, h0, h1);
     }
-    reduce_bn<3>(acc, g, t.active, red, RoundFinBn{red, evals_out, LANE_HG ? nullptr : vx, g.N});
+    reduce_bn<3>(acc, g, t.active, red, RoundFinBn{evals_out, LANE_HG ? nullptr : vx, g.N});
 }
 
 __global__ void k_s_build(uint64_t I, const uint32_t* __restrict__ my_off, const uint4* __restrict__ my_g,
@@ -699,7 +709,7 @@ __global__ void __launch_bounds__(256) k_wsum(const uint32_t* __restrict__ vals,
     if (t.active)
         for (uint64_t z = (uint64_t)blockIdx.x * g.rps + t.rs; z < rows; z += (uint64_t)gridDim.x * g.rps)
             acc[0] = add(acc[0], mul(lds(eq, z), ldf(vals, z, g.N, t.q)));
-    reduce_bn<1>(acc, g, t.active, red, CopyFinBn{red, out, g.N});
+    reduce_bn<1>(acc, g, t.active, red, CopyFinBn{out, g.N});
 }
 
 uint32_t grid1(uint64_t n) {
