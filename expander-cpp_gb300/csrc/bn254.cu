@@ -286,7 +286,7 @@ __device__ __forceinline__ Tile tile(const GeoBn& g) {
 }
 
 // Canonical total of component c of one lane; leaves its accumulators zeroed.
-__device__ __forceinline__ Fr take(const RedBn& red, uint32_t c, uint32_t N, uint32_t lane) {
+__device__ __noinline__ Fr take(const RedBn& red, uint32_t c, uint32_t N, uint32_t lane) {
     unsigned long long s[8];
     unsigned long long* p = &red.acc[((size_t)c * N + lane) * 8];
 #pragma unroll
@@ -377,7 +377,7 @@ struct RoundFinBn {
     uint32_t* out;  // 3 x N x 8 limbs, canonical
     const uint32_t* vx;
     uint32_t N;
-    __device__ void operator()(uint32_t c, uint32_t lane, const Fr* t, uint32_t tpr) const {
+    __device__ __noinline__ void operator()(uint32_t c, uint32_t lane, const Fr* t, uint32_t tpr) const {
         Fr v;
         if (c < 2) {
             v = t[c * tpr];
@@ -605,16 +605,20 @@ __global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ 
     Fr acc[3] = {zero(), zero(), zero()};
     if (t.active) {
         for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < (I >> 1); i += (uint64_t)gridDim.x * g.rps) {
-            Fr h[2];
-#pragma unroll
+            Fr h0, h1;
+            // not unrolled: each copy of the gate loop inlines a 256-bit product, and two of
+            // them left this kernel waiting on instruction fetch (ncu: no_instruction stalls)
+#pragma unroll 1
             for (int s = 0; s < 2; s++) {
                 const uint64_t x = 2 * i + s;
-                h[s] = lds(a, x);
+                Fr h = lds(a, x);
                 const uint32_t k0 = __ldg(mx_off + x), k1 = __ldg(mx_off + x + 1);
-                for (uint32_t k = k0; k < k1; k++) h[s] = add(h[s], mul(ldf(v, __ldg(&mx_g[k].x), g.N, t.q), lds(w, k)));
-                stf(hg, x, g.N, t.q, h[s]);
+                for (uint32_t k = k0; k < k1; k++) h = add(h, mul(ldf(v, __ldg(&mx_g[k].x), g.N, t.q), lds(w, k)));
+                stf(hg, x, g.N, t.q, h);
+                if (s == 0) h0 = h;
+                else h1 = h;
             }
-            accum(acc, ldf(v, 2 * i, g.N, t.q), ldf(v, 2 * i + 1, g.N, t.q), h[0], h[1]);
+            accum(acc, ldf(v, 2 * i, g.N, t.q), ldf(v, 2 * i + 1, g.N, t.q), h0, h1);
         }
     }
     reduce_bn<3>(acc, g, t.active, red, RoundFinBn{evals_out, nullptr, g.N});

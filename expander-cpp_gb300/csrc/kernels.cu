@@ -594,26 +594,40 @@ __global__ void __launch_bounds__(256) k_p2_round0(RoundPtrs p, uint64_t npairs,
     const uint2* __restrict__ sj =
         reinterpret_cast<const uint2*>(j == 0 ? p.hsrc[0] : (j == 1 ? p.hsrc[1] : p.hsrc[2]));
     uint64_t acc[3][4] = {};
+    auto pair = [&](const uint4& a0, const uint4& a1, const uint2& s) {
+        const uint32_t s01 = add(s.x, s.y);
+#pragma unroll
+        for (int l = 0; l < 4; l++) {
+            acc[0][l] += (uint64_t)comp(a0, l) * s.x;
+            acc[1][l] += (uint64_t)comp(a1, l) * s.y;
+            acc[2][l] += (uint64_t)add(comp(a0, l), comp(a1, l)) * s01;
+        }
+    };
+    // each product is < 2^62: after a fold (< 2^34) three more keep the sum < 2^64
+    auto fold_acc = [&]() {
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+#pragma unroll
+            for (int l = 0; l < 4; l++) acc[c][l] = (acc[c][l] & m31::P) + (acc[c][l] >> 31);
+    };
     if (t.active) {
-        uint32_t since_fold = 0;
-        for (uint64_t i = (uint64_t)cx * g.rps + t.rs; i < npairs; i += (uint64_t)nx * g.rps) {
+        const uint64_t step = (uint64_t)nx * g.rps;
+        uint64_t i = (uint64_t)cx * g.rps + t.rs;
+        // three pairs per iteration: their six row loads are in flight together
+        for (; i + 2 * step < npairs; i += 3 * step) {
+            const uint64_t i1 = i + step, i2 = i + 2 * step;
             const uint4 a0 = ld4(fs, 2 * i, g.N, t.lane0), a1 = ld4(fs, 2 * i + 1, g.N, t.lane0);
-            const uint2 s = __ldg(sj + i);
-            const uint32_t s01 = add(s.x, s.y);
-#pragma unroll
-            for (int l = 0; l < 4; l++) {
-                acc[0][l] += (uint64_t)comp(a0, l) * s.x;
-                acc[1][l] += (uint64_t)comp(a1, l) * s.y;
-                acc[2][l] += (uint64_t)add(comp(a0, l), comp(a1, l)) * s01;
-            }
-            // each product is < 2^62: after a fold (< 2^34) three more keep the sum < 2^64
-            if (++since_fold == 3) {
-                since_fold = 0;
-#pragma unroll
-                for (int c = 0; c < 3; c++)
-#pragma unroll
-                    for (int l = 0; l < 4; l++) acc[c][l] = (acc[c][l] & m31::P) + (acc[c][l] >> 31);
-            }
+            const uint4 b0 = ld4(fs, 2 * i1, g.N, t.lane0), b1 = ld4(fs, 2 * i1 + 1, g.N, t.lane0);
+            const uint4 c0 = ld4(fs, 2 * i2, g.N, t.lane0), c1 = ld4(fs, 2 * i2 + 1, g.N, t.lane0);
+            const uint2 sa = __ldg(sj + i), sb = __ldg(sj + i1), sc = __ldg(sj + i2);
+            pair(a0, a1, sa);
+            pair(b0, b1, sb);
+            pair(c0, c1, sc);
+            fold_acc();
+        }
+        for (; i < npairs; i += step) {
+            pair(ld4(fs, 2 * i, g.N, t.lane0), ld4(fs, 2 * i + 1, g.N, t.lane0), __ldg(sj + i));
+            fold_acc();
         }
     }
     uint32_t out[3][4];
