@@ -195,6 +195,7 @@ struct gkrgpu_job {
     const gkrgpu_circuit* circuit = nullptr;
     uint32_t N = 0;
     int grinding = 10, R = 3, marker = -1;
+    int fs_hash = kFsSha256;  // transcript hash (FiatShamir_hash_type)
     const uint32_t* h_input = nullptr;
     const uint32_t* d_input = nullptr;
     uint8_t* proof_out = nullptr;
@@ -341,6 +342,7 @@ struct gkrgpu_ctx {
     std::vector<std::thread> workers;
     std::vector<std::unique_ptr<Lane>> lanes;
     int n_lanes = 1, host_workers = 2, running = 0;
+    int fs_hash = kFsSha256;  // transcript hash of jobs submitted from now on
     bool stopping = false;
 
     void start_workers();
@@ -1039,7 +1041,7 @@ uint64_t proof_bytes(const gkrgpu_circuit* c, uint32_t N, int R) {
 // worker takes the next queued device stage once the proof's workspace fits the budget.
 
 // Copies n bytes in helper threads while this thread hashes the source.
-void parallel_copy_and_hash(uint8_t* dst, const uint8_t* src, uint64_t n, uint8_t digest[32]) {
+void parallel_copy_and_hash(uint8_t* dst, const uint8_t* src, uint64_t n, int hash, uint8_t digest[32]) {
     const unsigned k = n >= (64ull << 20) ? 4 : (n >= (4ull << 20) ? 2 : 0);
     std::vector<std::thread> th;
     if (k) {
@@ -1051,7 +1053,7 @@ void parallel_copy_and_hash(uint8_t* dst, const uint8_t* src, uint64_t n, uint8_
     } else {
         memcpy(dst, src, n);
     }
-    sha256(src, n, digest);
+    fs_hash(hash, src, n, digest);
     for (auto& t : th) t.join();
 }
 
@@ -1060,14 +1062,14 @@ TranscriptState host_stage(gkrgpu_ctx& c, gkrgpu_job& j, cudaStream_t s) {
     const uint64_t in_bytes = j.circuit->in_rows(0) * (uint64_t)j.N * elem_bytes(j.circuit->field);
     uint8_t d[32];
     if (j.h_input) {
-        parallel_copy_and_hash(j.proof_out, reinterpret_cast<const uint8_t*>(j.h_input), in_bytes, d);
+        parallel_copy_and_hash(j.proof_out, reinterpret_cast<const uint8_t*>(j.h_input), in_bytes, j.fs_hash, d);
     } else {
         ck(cudaMemcpyAsync(j.proof_out, j.d_input, in_bytes, cudaMemcpyDeviceToHost, s), "commitment readback");
         ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
         c.d2h_bytes += in_bytes;
-        sha256(j.proof_out, in_bytes, d);
+        fs_hash(j.fs_hash, j.proof_out, in_bytes, d);
     }
-    Transcript t(j.proof_out, ~0ull);
+    Transcript t(j.proof_out, ~0ull, j.fs_hash);
     t.appended_prehashed(in_bytes, d);
     if (bn)
         grind_bn254(t, j.grinding);
@@ -1205,6 +1207,7 @@ gkrgpu_job* submit(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_co
     j->proof_len = need;
     j->claimed_v = claimed_v;
     j->marker = marker;
+    j->fs_hash = ctx->fs_hash;
     ctx->start_workers();
     {
         std::lock_guard<std::mutex> lk(ctx->qm);
@@ -1462,6 +1465,16 @@ int gkrgpu_prove_device(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
     }
     return prove_entry(ctx, circuit, n_copies, grinding_bits, nullptr, d_input, proof_out, proof_cap, proof_len,
                        claimed_v);
+}
+
+int gkrgpu_set_fs_hash(gkrgpu_ctx* ctx, int fs_hash_type) {
+    return guarded([&] {
+        check_ctx(ctx);
+        if (fs_hash_type != kFsSha256 && fs_hash_type != kFsKeccak256)
+            fail(GKRGPU_ERR_INVALID, "unsupported transcript hash %d (SHA256 = 0, Keccak256 = 1)", fs_hash_type);
+        ctx->drain();
+        ctx->fs_hash = fs_hash_type;
+    });
 }
 
 int gkrgpu_verify(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,

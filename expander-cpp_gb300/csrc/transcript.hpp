@@ -5,25 +5,42 @@
 // was appended (:91-103) - the digest is not chained into new data.  The digest starts
 // as 32 zero bytes (:118-125).  challenge_f reads the first 4 digest bytes as a
 // little-endian u32 and reduces it mod p (M31::from_bytes, include/field/M31.hpp:111-116).
+//
+// The hash is SHA-256, the only one the reference's transcript implements (the prover
+// asserts it, include/LinearGKR/LinearGKR.hpp:45).  Config::FS_hash also names Keccak256
+// (include/configuration/config.hpp:18-24) without code behind it; selecting it here runs
+// the same schedule with Keccak-256 (keccak.hpp) in every place SHA-256 is used.
 #pragma once
 #include <stdint.h>
 #include <string.h>
 
 #include "fr_host.hpp"
+#include "keccak.hpp"
 #include "m31.cuh"
 #include "sha256.hpp"
 
 namespace gkrgpu {
 
-// Position of a transcript: bytes written, start of the not-yet-hashed bytes, digest.
+// FiatShamir_hash_type numbering (config.hpp:18-24).
+enum FsHash : int { kFsSha256 = 0, kFsKeccak256 = 1 };
+
+inline void fs_hash(int h, const uint8_t* p, uint64_t n, uint8_t out[32]) {
+    if (h == kFsKeccak256)
+        keccak256(p, (size_t)n, out);
+    else
+        sha256(p, n, out);
+}
+
+// Position of a transcript: bytes written, start of the not-yet-hashed bytes, digest, hash.
 struct TranscriptState {
     uint64_t len = 0, hash_start = 0;
     uint8_t digest[32] = {};
+    int hash = kFsSha256;
 };
 
 class Transcript {
    public:
-    Transcript(uint8_t* buf, uint64_t cap) : buf_(buf), cap_(cap) {}
+    Transcript(uint8_t* buf, uint64_t cap, int hash = kFsSha256) : buf_(buf), cap_(cap) { s_.hash = hash; }
     // Resumes a transcript over the same buffer (e.g. on another thread).
     Transcript(uint8_t* buf, const TranscriptState& s) : buf_(buf), cap_(~0ull), s_(s) {}
 
@@ -52,7 +69,7 @@ class Transcript {
     // append+challenge steps would when nothing else is pending; the three SHA-256 run
     // interleaved.  Returns false (and does nothing) when bytes are pending.
     bool append_challenge3(const uint8_t* const msgs[3], uint64_t n, uint32_t out[3]) {
-        if (s_.len != s_.hash_start || has_pre_) return false;
+        if (s_.len != s_.hash_start || has_pre_ || s_.hash != kFsSha256) return false;
         const uint8_t* at[3];
         for (int m = 0; m < 3; m++) {
             at[m] = buf_ + s_.len;
@@ -85,11 +102,11 @@ class Transcript {
             s_.hash_start = s_.len;
             has_pre_ = false;
         } else if (s_.len > s_.hash_start) {
-            sha256(buf_ + s_.hash_start, s_.len - s_.hash_start, s_.digest);
+            fs_hash(s_.hash, buf_ + s_.hash_start, s_.len - s_.hash_start, s_.digest);
             s_.hash_start = s_.len;
         } else {
             uint8_t d[32];
-            sha256(s_.digest, 32, d);
+            fs_hash(s_.hash, s_.digest, 32, d);
             memcpy(s_.digest, d, 32);
         }
         return s_.digest;
@@ -115,7 +132,7 @@ inline void grind(Transcript& t, int grinding_bits) {
     }
     for (long i = 0; i < (1L << grinding_bits); i++) {
         uint8_t d[32];
-        sha256(h, 32, d);
+        fs_hash(t.state().hash, h, 32, d);
         memcpy(h, d, 32);
     }
     t.append(h, 32);
@@ -127,7 +144,7 @@ inline void grind_bn254(Transcript& t, int grinding_bits) {
     frh::to_bytes(t.challenge_bn254(), h);
     for (long i = 0; i < (1L << grinding_bits); i++) {
         uint8_t d[32];
-        sha256(h, 32, d);
+        fs_hash(t.state().hash, h, 32, d);
         memcpy(h, d, 32);
     }
     t.append(h, 32);

@@ -118,9 +118,9 @@ struct Verifier {
 
         // transcript: the commitment bytes (hashed in place), grinding
         std::unique_ptr<uint8_t[]> tbuf(new uint8_t[len + 64]);
-        Transcript t(tbuf.get(), len + 64);
+        Transcript t(tbuf.get(), len + 64, X.fs_hash);
         uint8_t d[32];
-        sha256(proof, com_bytes, d);
+        fs_hash(X.fs_hash, proof, com_bytes, d);
         t.appended_prehashed(com_bytes, d);
         grind(t, grinding_bits);
         uint64_t pos = com_bytes + 32;
@@ -315,9 +315,9 @@ struct BnVerifier {
                  [&] { return bn::launch_load(raw, com, C.in_rows(0) * N, nullptr, c.stream); });
 
         std::unique_ptr<uint8_t[]> tbuf(new uint8_t[len + 64]);
-        Transcript t(tbuf.get(), len + 64);
+        Transcript t(tbuf.get(), len + 64, X.fs_hash);
         uint8_t d[32];
-        sha256(proof, com_bytes, d);
+        fs_hash(X.fs_hash, proof, com_bytes, d);
         t.appended_prehashed(com_bytes, d);
         grind_bn254(t, grinding_bits);
         uint64_t pos = com_bytes + 32;

@@ -13,6 +13,8 @@ OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_CAPACITY, ERR_TIMEOUT, ERR_STATE = ran
 
 # Field_type numbering of include/configuration/config.hpp:12-16 (GKRGPU_FIELD_*).
 FIELDS = {"M31": 0, "BabyBear": 1, "BN254": 2}
+# FiatShamir_hash_type numbering (include/configuration/config.hpp:18-24)
+FS_HASHES = {"SHA256": 0, "Keccak256": 1}
 
 
 class GkrGpuError(RuntimeError):
@@ -71,6 +73,9 @@ SIGNATURES = [
     ("gkrgpu_prove_submit", _I, [_P, _P, _U32, _I, _P, _I, _P, _U64, _P, _I, ctypes.POINTER(_P)]),
     ("gkrgpu_prove_wait", _I, [_P, ctypes.POINTER(_U64)]),
     ("gkrgpu_verify", _I, [_P, _P, _U32, _I, _P, _U64, _P, ctypes.POINTER(_I)]),
+    ("gkrgpu_set_fs_hash", _I, [_P, _I]),
+    ("gkrgpu_keccak256", None, [_P, _U64, _P]),
+    ("gkrgpu_sha3_256", None, [_P, _U64, _P]),
     ("gkrgpu_set_concurrency", _I, [_P, _I, _U64]),
     ("gkrgpu_workspace_bytes", _U64, [_P, _U32, _I, _I]),
     ("gkrgpu_memory_stats", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
@@ -116,3 +121,20 @@ def check(rc):
         msg = load().gkrgpu_last_error()
         raise GkrGpuError(rc, msg.decode() if msg else "")
     return rc
+
+
+def _digest(fn, data: bytes) -> bytes:
+    buf = (ctypes.c_uint8 * max(len(data), 1)).from_buffer_copy(data or b"\0")
+    out = (ctypes.c_uint8 * 32)()
+    fn(buf, len(data), out)
+    return bytes(out)
+
+
+def keccak256(data: bytes) -> bytes:
+    """Keccak-256 as the transcript uses it (host-side, gkrgpu_keccak256)."""
+    return _digest(load().gkrgpu_keccak256, bytes(data))
+
+
+def sha3_256(data: bytes) -> bytes:
+    """SHA3-256 over the same Keccak-f[1600] sponge (gkrgpu_sha3_256)."""
+    return _digest(load().gkrgpu_sha3_256, bytes(data))

@@ -22,8 +22,9 @@ if platform.machine() in ("aarch64", "arm64"):
     # ARMv8 SHA-2 instructions for the transcript hash (all Neoverse cores have them).
     CXXFLAGS.append("-march=armv8.2-a+crypto")
 
-SOURCES = ["kernels.cu", "prover.cu", "sha256.cpp", "noalloc.cu", "bn254.cu", "circuit2.cpp"]
-HEADERS = ["kernels.cuh", "m31.cuh", "sha256.hpp", "transcript.hpp", "bn254.cuh", "bn254_prover.cuh", "fr_host.hpp"]
+SOURCES = ["kernels.cu", "prover.cu", "sha256.cpp", "noalloc.cu", "bn254.cu", "circuit2.cpp", "keccak.cpp"]
+HEADERS = ["kernels.cuh", "m31.cuh", "sha256.hpp", "transcript.hpp", "bn254.cuh", "bn254_prover.cuh", "fr_host.hpp",
+           "verifier.cuh", "keccak.hpp"]
 
 
 def _deps():

@@ -20,18 +20,20 @@ from .circuit import Circuit
 
 
 class Config:
-    """Config of the reference: 100-bit security, RAW commitment, SHA-256 transcript, field
-    M31 (default) or BN254 (config.hpp:12-16,40-86)."""
+    """Config of the reference: 100-bit security, RAW commitment, field M31 (default) or BN254,
+    transcript hash SHA256 (default, the reference's) or Keccak256 (config.hpp:12-24,40-86)."""
 
-    def __init__(self, grinding_bits: int = 10, field_type: str = "M31"):
+    def __init__(self, grinding_bits: int = 10, field_type: str = "M31", FS_hash: str = "SHA256"):
         if field_type not in ("M31", "BN254"):
             raise ValueError(f"unsupported field_type {field_type!r} (M31 or BN254)")
+        if FS_hash not in _lib.FS_HASHES:
+            raise ValueError(f"unsupported FS_hash {FS_hash!r} (SHA256 or Keccak256)")
         self.security_bits = 100
         self.grinding_bits = int(grinding_bits)
         self.field_type = field_type
         self.field_size = 254 if field_type == "BN254" else 31
         self.PC_type = "Raw"
-        self.FS_hash = "SHA256"
+        self.FS_hash = FS_hash
 
     def get_num_repetitions(self) -> int:
         return _lib.load().gkrgpu_num_repetitions_field(_lib.FIELDS[self.field_type], self.grinding_bits)
@@ -130,6 +132,7 @@ class Context:
         _lib.check(lib.gkrgpu_create(device, ctypes.byref(h)))
         self.handle = h
         self.device = device
+        self.fs_hash = "SHA256"
 
     def close(self):
         if getattr(self, "handle", None):
@@ -144,6 +147,15 @@ class Context:
 
     def load(self, circuit: Circuit, field: str = "M31") -> DeviceCircuit:
         return DeviceCircuit(self, circuit, field)
+
+    def set_fs_hash(self, name: str):
+        """Transcript hash of later proofs and verifications: "SHA256" (the reference's) or
+        "Keccak256" (gkrgpu_set_fs_hash; waits for queued proofs)."""
+        if name not in _lib.FS_HASHES:
+            raise ValueError(f"unsupported FS_hash {name!r} (SHA256 or Keccak256)")
+        if name != self.fs_hash:
+            _lib.check(_lib.load().gkrgpu_set_fs_hash(self.handle, _lib.FS_HASHES[name]))
+            self.fs_hash = name
 
     def evaluate(self, dc: DeviceCircuit, witness, all_layers=False):
         """Circuit::evaluate on the device; returns the output rows, or with all_layers every
@@ -355,13 +367,14 @@ class Prover:
         w = circuit.input_values if witness is None else witness
         if w is None:
             raise ValueError("no circuit input: call circuit.set_input(values) or pass witness")
+        self.ctx.set_fs_hash(self.config.FS_hash)
         cv, proof = self.ctx.prove(self._dc, w, self.config.grinding_bits)
         return cv, Proof(proof)
 
 
 class Verifier:
     """gkr::Verifier (include/LinearGKR/LinearGKR.hpp:92-149) with its device-side parts on the
-    GPU (gkrgpu_verify); M31 circuits."""
+    GPU (gkrgpu_verify); M31 and BN254 circuits."""
 
     def __init__(self, config: Config = None, ctx: Context = None):
         self.config = config or Config()
@@ -374,4 +387,5 @@ class Verifier:
             self._dc = self.ctx.load(circuit, self.config.field_type)
             self._circuit = circuit
         data = proof.bytes if isinstance(proof, Proof) else proof
+        self.ctx.set_fs_hash(self.config.FS_hash)
         return self.ctx.verify(self._dc, data, claimed_v, self.config.grinding_bits)

@@ -153,6 +153,22 @@ int gkrgpu_prove_device(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
                         const uint32_t* d_input, uint8_t* proof_out, uint64_t proof_cap, uint64_t* proof_len,
                         uint32_t* claimed_v);
 
+/* Transcript hash of the proofs submitted on this context from now on and of
+ * gkrgpu_verify (FiatShamir_hash_type numbering, include/configuration/config.hpp:18-24):
+ * GKRGPU_FS_SHA256 (default; the only hash the reference's transcript implements, so the
+ * only one with byte parity against it) or GKRGPU_FS_KECCAK256 (the same transcript schedule
+ * with Keccak-256 wherever SHA-256 is used; the reference has no Keccak code).  Waits for
+ * queued proofs first. */
+#define GKRGPU_FS_SHA256 0
+#define GKRGPU_FS_KECCAK256 1
+int gkrgpu_set_fs_hash(gkrgpu_ctx* ctx, int fs_hash_type);
+
+/* The Keccak-256 transcript hash (original Keccak padding, domain byte 0x01, rate 136
+ * bytes) and SHA3-256 (the same sponge with the FIPS 202 domain byte 0x06), host-side;
+ * out receives 32 bytes. */
+void gkrgpu_keccak256(const uint8_t* in, uint64_t len, uint8_t* out);
+void gkrgpu_sha3_256(const uint8_t* in, uint64_t len, uint8_t* out);
+
 /* Verifier::verify (include/LinearGKR/LinearGKR.hpp:105-149: gkr_verify, gkr.hpp:75-122, and
  * RawPC::verify, raw.hpp:75-78), GPU-assisted, for M31 and BN254 circuits: the host replays the
  * transcript and checks every round; the device computes each layer's

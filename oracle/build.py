@@ -22,13 +22,14 @@ def _stale(target, sources):
 
 
 def build_oracle(force=False):
-    srcs = [os.path.join(HERE, f) for f in ("gkr_oracle.c", "gkr_oracle_bn254.c", "gkr_oracle.h", "bn254.h")]
+    srcs = [os.path.join(HERE, f) for f in ("gkr_oracle.c", "gkr_oracle_bn254.c", "fs_hash.c", "gkr_oracle.h",
+                                            "bn254.h")]
     if not force and not _stale(ORACLE_SO, srcs):
         return ORACLE_SO
     os.makedirs(BUILD, exist_ok=True)
     tmp = ORACLE_SO + ".tmp"
     subprocess.check_call(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-pthread", "-Wall",
-                           srcs[0], srcs[1], "-o", tmp])
+                           srcs[0], srcs[1], srcs[2], "-o", tmp])
     os.replace(tmp, ORACLE_SO)
     return ORACLE_SO
 

@@ -104,10 +104,10 @@ static void tr_append(transcript* t, const void* p, uint64_t n) {
 }
 static void tr_hash_to_digest(transcript* t) {
     if (t->len > t->hash_start) {
-        oracle_sha256(t->bytes + t->hash_start, t->len - t->hash_start, t->digest);
+        oracle_fs_hash(t->bytes + t->hash_start, t->len - t->hash_start, t->digest);
         t->hash_start = t->len;
     } else {
-        oracle_sha256(t->digest, 32, t->digest);
+        oracle_fs_hash(t->digest, 32, t->digest);
     }
 }
 /* Transcript::challenge_f, :139-147: M31::from_bytes of the digest's first 4 bytes. */
@@ -127,7 +127,7 @@ static void grind(transcript* t, int grinding_bits) {
         uint32_t c = tr_challenge(t);
         memcpy(h + 4 * i, &c, 4);
     }
-    for (long i = 0; i < (1L << grinding_bits); i++) oracle_sha256(h, 32, h);
+    for (long i = 0; i < (1L << grinding_bits); i++) oracle_fs_hash(h, 32, h);
     tr_append(t, h, 32);
 }
 

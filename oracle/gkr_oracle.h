@@ -54,6 +54,14 @@ void oracle_eval_multilinear(const uint32_t* evals, uint32_t nb_vars, uint32_t n
 /* SHA256Hasher::hash (include/hash/hashes.hpp:22-33). */
 void oracle_sha256(const uint8_t* in, uint64_t len, uint8_t out[32]);
 
+/* Transcript hash selection (fs_hash.c): 0 = SHA-256 (default), 1 = Keccak-256; process-wide,
+ * for single-threaded test use.  oracle_fs_hash hashes with the selected function. */
+void oracle_set_fs_hash(int h);
+int oracle_get_fs_hash(void);
+void oracle_fs_hash(const uint8_t* in, uint64_t len, uint8_t out[32]);
+void oracle_keccak256(const uint8_t* in, uint64_t len, uint8_t out[32]);
+void oracle_sha3_256(const uint8_t* in, uint64_t len, uint8_t out[32]);
+
 /* Throughput harness in the manner of benchmarks/bench_keccak.cpp:32-42,82-93: n_threads
  * threads each run proofs_per_thread proofs (evaluate + prove) of the same circuit.
  * Returns wall seconds, or a negative value on failure. */

@@ -74,10 +74,10 @@ static void tr_append_row(tr_t* t, const fe* row, uint32_t N) {
 }
 static void tr_hash_to_digest(tr_t* t) {
     if (t->len > t->hash_start) {
-        oracle_sha256(t->bytes + t->hash_start, t->len - t->hash_start, t->digest);
+        oracle_fs_hash(t->bytes + t->hash_start, t->len - t->hash_start, t->digest);
         t->hash_start = t->len;
     } else {
-        oracle_sha256(t->digest, 32, t->digest);
+        oracle_fs_hash(t->digest, 32, t->digest);
     }
 }
 /* challenge_f: the digest read little-endian, reduced mod r (canonical). */
@@ -89,7 +89,7 @@ static fe tr_challenge(tr_t* t) {
 static void grind(tr_t* t, int grinding_bits) {
     uint8_t h[32];
     bn_to_bytes(tr_challenge(t), h);
-    for (long i = 0; i < (1L << grinding_bits); i++) oracle_sha256(h, 32, h);
+    for (long i = 0; i < (1L << grinding_bits); i++) oracle_fs_hash(h, 32, h);
     tr_append(t, h, 32);
 }
 

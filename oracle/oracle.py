@@ -41,7 +41,31 @@ def proof_size(circuit, n_copies, reps):
     return (1 << circuit.layers[0].nb_input_vars) * n_copies * 4 + 32 + rows * n_copies * 4
 
 
-class Oracle:
+FS_HASHES = {"SHA256": 0, "Keccak256": 1}
+
+
+class _FsHash:
+    """Transcript-hash selection and the Keccak sponge of oracle/fs_hash.c (process-wide)."""
+
+    def set_fs_hash(self, name: str):
+        self.lib.oracle_set_fs_hash.argtypes = [ctypes.c_int]
+        self.lib.oracle_set_fs_hash(FS_HASHES[name])
+
+    def _digest(self, fn, data):
+        b = np.frombuffer(bytes(data), np.uint8)
+        out = np.empty(32, np.uint8)
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
+        fn(b.ctypes.data if len(b) else None, len(b), out.ctypes.data)
+        return out.tobytes()
+
+    def keccak256(self, data: bytes) -> bytes:
+        return self._digest(self.lib.oracle_keccak256, data)
+
+    def sha3_256(self, data: bytes) -> bytes:
+        return self._digest(self.lib.oracle_sha3_256, data)
+
+
+class Oracle(_FsHash):
     """The C restatement of the reference prover/verifier."""
 
     def __init__(self, path=None):
@@ -122,7 +146,7 @@ class Oracle:
         return t
 
 
-class OracleBn254:
+class OracleBn254(_FsHash):
     """The C restatement over BN254 (oracle/gkr_oracle_bn254.c).  Tables are (rows, N, 4)
     uint64 limb arrays; claimed_v is (1, N, 4)."""
 
