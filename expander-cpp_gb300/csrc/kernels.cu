@@ -277,10 +277,13 @@ struct RoundFin {
     uint32_t* out;       // R x 3 x N
     const uint32_t* vx;  // R x N, or null
     uint32_t N, reps;
+    bool cross = false;  // component 2 holds sum f0 h1 + f1 h0 instead of p2raw
     __device__ void operator()(uint32_t lane) const {
         for (uint32_t j = 0; j < reps; j++) {
             uint32_t p0 = take(red, 3 * j, N, lane), p1 = take(red, 3 * j + 1, N, lane);
-            uint32_t p2 = m31::eval_at_two(p0, p1, take(red, 3 * j + 2, N, lane));
+            uint32_t c2 = take(red, 3 * j + 2, N, lane);
+            if (cross) c2 = add(add(p0, p1), c2);
+            uint32_t p2 = m31::eval_at_two(p0, p1, c2);
             if (vx) {
                 const uint32_t x = vx[(size_t)j * N + lane];
                 p0 = mul(p0, x); p1 = mul(p1, x); p2 = mul(p2, x);
@@ -311,60 +314,126 @@ __device__ __forceinline__ void accum_pair(uint32_t (&acc)[3][4], const uint32_t
     }
 }
 
+// ---------------------------------------------------------------- asynchronous row staging
+// cp.async copies (global -> shared, no registers held while in flight) let a thread keep
+// several iterations' rows in flight.  Each thread copies and later reads back only its
+// own slots, so no barrier is needed between threads; a slot is refilled only after the
+// values read from it have been used.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int K>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(K) : "memory");
+}
+
 // ---------------------------------------------------------------- phase one: hg build + round 0
 // For each pair (x0, x1) = (2i, 2i+1): hg_j[x] = a_j[x] + sum over mul gates (x, y, k) of
-// v[y] * w_j[k], then the round-0 sums of v(x) hg_j(x).  The table is written only when
-// hg0 is given: the prover rebuilds it inside round 1 (k_hg_round1) instead, which costs
-// the gathers again but saves writing and re-reading R full-width tables.
-// All repetitions in one thread: each gathered v[y] row serves the R weights.
+// v[y] * w_j[k], then the round-0 sums of v(x) hg_j(x).  hg is not stored: round 1
+// (k_hg_round1) rebuilds it, which costs the gathers again but saves writing and re-reading
+// R full-width tables.  All repetitions in one thread: each gathered v[y] row serves the R
+// weights.
+// The round reads 4 bytes per copy and row and is bound by integer instructions, so the
+// sums are kept as p0 = sum f0 h0, p1 = sum f1 h1 and the cross term pc = sum f0 h1 + f1 h0
+// (p2raw = sum (f0 + f1)(h0 + h1) = p0 + p1 + pc, formed by the finisher), each product
+// added with mac_lazy (no reduction to canonical form), h of one row live at a time; a row
+// without mul gates (most rows of a wide layer) takes hg_j = a_j directly.  The pair's two
+// input rows, their add-gate weights and CSR offsets are staged by cp.async kStages - 1
+// iterations ahead.
+constexpr int kStages = 3;
+constexpr int kStageFields = 5;  // v(2i), v(2i+1), a(2i), a(2i+1), (off(2i), off(2i+1), off(2i+2))
+
 template <int R>
-__global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ v, uint64_t I,
-                                                      const uint32_t* __restrict__ mx_off, const uint4* __restrict__ mx_g,
-                                                      const uint4* __restrict__ a4, const uint4* __restrict__ w4,
-                                                      uint32_t* hg0, uint32_t* hg1, uint32_t* hg2, Geo g,
-                                                      RedScratch red, uint32_t* evals_out) {
+__global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict__ v, uint64_t I,
+                                                      const uint32_t* __restrict__ mx_off,
+                                                      const uint4* __restrict__ mx_g, const uint4* __restrict__ a4,
+                                                      const uint4* __restrict__ w4, Geo g, RedScratch red,
+                                                      uint32_t* evals_out) {
+    extern __shared__ uint4 ring[];  // kStages x kStageFields x blockDim.x
     const TileIdx t = tile_idx(g);
-    uint32_t acc[3 * R][4] = {};
-    uint32_t* hg[3] = {hg0, hg1, hg2};
-    if (t.active) {
-        const uint64_t npairs = I >> 1;
-        for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
-            uint32_t h[2][R][4];
+    const uint32_t B = blockDim.x, tid = threadIdx.x;
+    uint32_t acc[3 * R][4];
 #pragma unroll
-            for (int s = 0; s < 2; s++) {
-                const uint64_t x = 2 * i + s;
-                const uint4 a = __ldg(a4 + x);
+    for (int c = 0; c < 3 * R; c++)
 #pragma unroll
-                for (int j = 0; j < R; j++)
-#pragma unroll
-                    for (int l = 0; l < 4; l++) h[s][j][l] = comp(a, j);
-                const uint32_t k0 = __ldg(mx_off + x), k1 = __ldg(mx_off + x + 1);
-                for (uint32_t k = k0; k < k1; k++) {
-                    const uint32_t y = __ldg(&mx_g[k].x);
-                    const uint4 w = __ldg(w4 + k);
-                    const uint4 vy = ld4(v, y, g.N, t.lane0);
-#pragma unroll
-                    for (int j = 0; j < R; j++)
-#pragma unroll
-                        for (int l = 0; l < 4; l++) h[s][j][l] = add(h[s][j][l], mul(comp(vy, l), comp(w, j)));
-                }
-                if (hg0)
-#pragma unroll
-                    for (int j = 0; j < R; j++) st4(hg[j], x, g.N, t.lane0, mk4(h[s][j]));
-            }
-            const uint4 v0 = ld4(v, 2 * i, g.N, t.lane0), v1 = ld4(v, 2 * i + 1, g.N, t.lane0);
+        for (int l = 0; l < 4; l++) acc[c][l] = 0u;
+    // row x of the pair (s = 0: x = 2i, s = 1: x = 2i+1): p_s += f_s h, pc += f_(1-s) h
+    auto row = [&](int s, const uint4& fs, const uint4& fo, const uint4& a, uint32_t k0, uint32_t k1) {
+        if (k0 == k1) {
 #pragma unroll
             for (int j = 0; j < R; j++)
 #pragma unroll
                 for (int l = 0; l < 4; l++) {
-                    const uint32_t f0 = comp(v0, l), f1 = comp(v1, l);
-                    acc[3 * j][l] = add(acc[3 * j][l], mul(f0, h[0][j][l]));
-                    acc[3 * j + 1][l] = add(acc[3 * j + 1][l], mul(f1, h[1][j][l]));
-                    acc[3 * j + 2][l] = add(acc[3 * j + 2][l], mul(add(f0, f1), add(h[0][j][l], h[1][j][l])));
+                    acc[3 * j + s][l] = m31::mac_lazy(acc[3 * j + s][l], comp(fs, l), comp(a, j));
+                    acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], comp(fo, l), comp(a, j));
                 }
+            return;
         }
+        uint32_t h[R][4];
+#pragma unroll
+        for (int j = 0; j < R; j++)
+#pragma unroll
+            for (int l = 0; l < 4; l++) h[j][l] = comp(a, j);
+        for (uint32_t k = k0; k < k1; k++) {
+            const uint32_t y = __ldg(&mx_g[k].x);
+            const uint4 w = __ldg(w4 + k);
+            const uint4 vy = ld4(v, y, g.N, t.lane0);
+#pragma unroll
+            for (int j = 0; j < R; j++)
+#pragma unroll
+                for (int l = 0; l < 4; l++) h[j][l] = m31::mac_lazy(h[j][l], comp(vy, l), comp(w, j));
+        }
+#pragma unroll
+        for (int j = 0; j < R; j++)
+#pragma unroll
+            for (int l = 0; l < 4; l++) {
+                const uint32_t hc = m31::from_u32(h[j][l]);
+                acc[3 * j + s][l] = m31::mac_lazy(acc[3 * j + s][l], comp(fs, l), hc);
+                acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], comp(fo, l), hc);
+            }
+    };
+    if (t.active) {
+        const uint64_t npairs = I >> 1, step = (uint64_t)gridDim.x * g.rps;
+        const uint64_t i0 = (uint64_t)blockIdx.x * g.rps + t.rs;
+        auto stage = [&](uint64_t i, int slot) {
+            if (i < npairs) {
+                uint4* st = ring + (size_t)slot * kStageFields * B + tid;
+                cp_async16(st, v + (2 * i) * g.N + t.lane0);
+                cp_async16(st + B, v + (2 * i + 1) * g.N + t.lane0);
+                cp_async16(st + 2 * B, a4 + 2 * i);
+                cp_async16(st + 3 * B, a4 + 2 * i + 1);
+                cp_async8(st + 4 * B, mx_off + 2 * i);
+                cp_async4(reinterpret_cast<uint32_t*>(st + 4 * B) + 2, mx_off + 2 * i + 2);
+            }
+            cp_async_commit();  // one group per iteration, empty past the end
+        };
+#pragma unroll
+        for (int s = 0; s < kStages - 1; s++) stage(i0 + s * step, s);
+        int slot = 0;
+        for (uint64_t i = i0; i < npairs; i += step) {
+            // refill the slot read in the previous iteration, then wait for this one
+            stage(i + (kStages - 1) * step, slot == 0 ? kStages - 1 : slot - 1);
+            cp_async_wait<kStages - 1>();
+            const uint4* st = ring + (size_t)slot * kStageFields * B + tid;
+            const uint4 f0 = st[0], f1 = st[B], off = st[4 * B];
+            row(0, f0, f1, st[2 * B], off.x, off.y);
+            row(1, f1, f0, st[3 * B], off.y, off.z);
+            slot = slot + 1 == kStages ? 0 : slot + 1;
+        }
+        cp_async_wait<0>();
     }
-    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R});
+    __syncthreads();  // the ring is reused as the reduction's scratch
+    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R, true});
 }
 
 // ---------------------------------------------------------------- phase one, round 1
@@ -754,16 +823,37 @@ cudaError_t launch_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* 
     return cudaGetLastError();
 }
 
+// Dynamic shared memory of the staged kernels: the cp.async ring, or the reduction's
+// scratch where that is larger (they share the allocation).
+template <class K>
+static size_t staged_smem(K kernel, size_t ring_bytes, size_t red_bytes) {
+    const size_t bytes = ring_bytes > red_bytes ? ring_bytes : red_bytes;
+    // above 48 KiB less the kernel's static shared memory the launch needs the opt-in
+    if (bytes > 40 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return bytes;
+}
+
 cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint32_t* mx_off, const uint4* mx_g,
-                             const uint4* a4, const uint4* w4, uint32_t* const hg[3], const Geo& g, uint32_t block,
-                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
-    LaunchShape sh = row_shape(g, I / 2, block, ctas, 3 * reps);
+                             const uint4* a4, const uint4* w4, const Geo& g, uint32_t block, uint32_t ctas,
+                             RedScratch red, uint32_t* evals_out, cudaStream_t s) {
+    // the kernel's launch bound is 256 threads: wider tiles are narrowed to it
+    Geo gb = g;
+    if (block > 256) block = 256;
+    while (gb.tpr > block && gb.tpr % 2 == 0) gb.tpr /= 2;
+    if (gb.tpr > block) return cudaErrorInvalidValue;
+    gb.rps = block / gb.tpr;
+    LaunchShape sh = row_shape(gb, I / 2, block, ctas, 3 * reps);
+    const size_t ring = (size_t)kStages * kStageFields * sizeof(uint4) * block;
+#define GKR_HG0(RR)                                                                                          \
+    k_hg_round0<RR><<<sh.grid, sh.block, staged_smem(k_hg_round0<RR>, ring, sh.smem), s>>>(v, I, mx_off, mx_g, a4, \
+                                                                                      w4, gb, red, evals_out)
     switch (reps) {
-        case 1: k_hg_round0<1><<<sh.grid, sh.block, sh.smem, s>>>(v, I, mx_off, mx_g, a4, w4, hg[0], hg[1], hg[2], g, red, evals_out); break;
-        case 2: k_hg_round0<2><<<sh.grid, sh.block, sh.smem, s>>>(v, I, mx_off, mx_g, a4, w4, hg[0], hg[1], hg[2], g, red, evals_out); break;
-        case 3: k_hg_round0<3><<<sh.grid, sh.block, sh.smem, s>>>(v, I, mx_off, mx_g, a4, w4, hg[0], hg[1], hg[2], g, red, evals_out); break;
+        case 1: GKR_HG0(1); break;
+        case 2: GKR_HG0(2); break;
+        case 3: GKR_HG0(3); break;
         default: return cudaErrorInvalidValue;
     }
+#undef GKR_HG0
     return cudaGetLastError();
 }
 

@@ -97,9 +97,10 @@ cudaError_t launch_eq(uint32_t* out, const EqArgs& a, cudaStream_t s);
 cudaError_t launch_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* eqc, const uint4* mx_g,
                            const uint32_t* ax_off, const uint2* ax_g, uint4* a_out, uint4* w_out, uint32_t reps,
                            cudaStream_t s);
+// Phase-one hg (not stored) and the round-0 evaluations.
 cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint32_t* mx_off, const uint4* mx_g,
-                             const uint4* a4, const uint4* w4, uint32_t* const hg[3], const Geo& g, uint32_t block,
-                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
+                             const uint4* a4, const uint4* w4, const Geo& g, uint32_t block, uint32_t ctas,
+                             RedScratch red, uint32_t* evals_out, cudaStream_t s);
 // Phase-one round 1 rebuilding hg from the gate weights (no stored hg table): outputs
 // p.fdst[j] / p.hdst[j] (I/2 rows each), challenges p.r[j]; npairs = I/4.
 cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* mx_off, const uint4* mx_g,

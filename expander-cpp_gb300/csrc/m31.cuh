@@ -46,6 +46,14 @@ GKR_HD uint32_t from_u32(uint32_t x) {
     return umin(s, s - P);
 }
 
+// acc + a * b (mod p) for any acc < 2^32 and canonical a, b, left unreduced below 2^32:
+// a * b <= (p - 1)^2 = 2^62 - 2^33 + 4, so t = acc + a * b < 2^62, t >> 31 < 2^31 and
+// (t & p) + (t >> 31) <= 2^32 - 2.  Chains of these stay below 2^32; from_u32 finishes.
+GKR_HD uint32_t mac_lazy(uint32_t acc, uint32_t a, uint32_t b) {
+    const uint64_t t = (uint64_t)a * b + acc;
+    return (uint32_t)(t & P) + (uint32_t)(t >> 31);
+}
+
 // a + (b - a) * r: the fold of a multilinear table at challenge r
 // (SumcheckMultiLinearProdHelper::receive_challenge, sumcheck_helper.hpp:115,124-125).
 GKR_HD uint32_t fold(uint32_t a, uint32_t b, uint32_t r) { return add(a, mul(sub(b, a), r)); }

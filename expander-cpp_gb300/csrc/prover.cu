@@ -830,10 +830,9 @@ struct Prover {
         });
         // round 0 only reduces hg; round 1 rebuilds it (k_hg_round1), so no full-width hg
         // table is ever written
-        uint32_t* hg[3] = {nullptr, nullptr, nullptr};
         const double hb = rb * (I + Ly.nmul) + 32.0 * Ly.nmul + 20.0 * I;
         c.launch(K_HG_ROUND0, hb, [&] {
-            return launch_hg_round0(R, v, I, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, hg, gk[K_HG_ROUND0], X.block,
+            return launch_hg_round0(R, v, I, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, gk[K_HG_ROUND0], X.block,
                                     ck_ctas[K_HG_ROUND0], red_mapped(), c.evals_d(), c.stream);
         });
         const uint32_t* vsrc[1] = {v};
@@ -841,7 +840,7 @@ struct Prover {
         transcript_round(t, rx, 0, n == 1, true, vxh);
 
         const uint32_t* cur_f[3] = {v, v, v};
-        const uint32_t* cur_h[3] = {hg[0], hg[1], hg[2]};
+        const uint32_t* cur_h[3] = {nullptr, nullptr, nullptr};  // round 1 rebuilds hg
         for (uint32_t k = 1; k < n; k++) {
             RoundPtrs p;
             memset(&p, 0, sizeof(p));
