@@ -442,68 +442,90 @@ __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict
 // and hg_j and the layer input are folded at r_j into rows 2i, 2i+1 of hdst_j / fdst_j
 // (what receive_challenge of round 0 would have left, sumcheck_helper.hpp:104-133), which
 // are stored and summed into the round-1 evaluations.  All repetitions in one thread, as in
-// k_hg_round0: each gathered v[y] row serves the R weights.  After the first half of a pair
-// only f and h of row 2i are kept (for the (f0 + f1)(h0 + h1) term).
+// k_hg_round0: each gathered v[y] row serves the R weights.  When neither source row of an
+// output row has mul gates, its hg is the same for every copy: fold(a_j[x0], a_j[x1], r_j)
+// is computed once.  The sums use the cross form of k_hg_round0 (p0, p1, pc with mac_lazy);
+// after the first row of a pair only its f and h are kept, for pc.
 template <int R>
 __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ v, uint64_t npairs,
                                                    const uint32_t* __restrict__ mx_off, const uint4* __restrict__ mx_g,
                                                    const uint4* __restrict__ a4, const uint4* __restrict__ w4,
                                                    RoundPtrs p, Geo g, RedScratch red, uint32_t* evals_out) {
     const TileIdx t = tile_idx(g);
-    uint32_t acc[3 * R][4] = {};
+    uint32_t acc[3 * R][4];
+#pragma unroll
+    for (int c = 0; c < 3 * R; c++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[c][l] = 0u;
     if (t.active) {
         for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
-            uint32_t f0[R][4], h0[R][4];
+            const uint4 o4 = __ldg(reinterpret_cast<const uint4*>(mx_off + 4 * i));  // off(4i .. 4i+3)
+            const uint32_t o_end = __ldg(mx_off + 4 * i + 4);
+            const uint32_t off[5] = {o4.x, o4.y, o4.z, o4.w, o_end};
+            uint32_t fe[R][4], he[R][4];
 #pragma unroll
             for (int s = 0; s < 2; s++) {
-                uint32_t hx[2][R][4];
+                const uint64_t x0 = 4 * i + 2 * s;
+                const uint4 v0 = ld4(v, x0, g.N, t.lane0), v1 = ld4(v, x0 + 1, g.N, t.lane0);
+                const uint4 a0 = __ldg(a4 + x0), a1 = __ldg(a4 + x0 + 1);
+                uint32_t h[R][4];
+                if (off[2 * s] == off[2 * s + 2]) {
 #pragma unroll
-                for (int e = 0; e < 2; e++) {
-                    const uint64_t x = 4 * i + 2 * s + e;
-                    const uint4 a = __ldg(a4 + x);
+                    for (int j = 0; j < R; j++) {
+                        const uint32_t hs = fold(comp(a0, j), comp(a1, j), p.r[j]);
 #pragma unroll
-                    for (int j = 0; j < R; j++)
+                        for (int l = 0; l < 4; l++) h[j][l] = hs;
+                    }
+                } else {
+                    uint32_t hx[2][R][4];
 #pragma unroll
-                        for (int l = 0; l < 4; l++) hx[e][j][l] = comp(a, j);
-                    const uint32_t k0 = __ldg(mx_off + x), k1 = __ldg(mx_off + x + 1);
-                    for (uint32_t k = k0; k < k1; k++) {
-                        const uint32_t y = __ldg(&mx_g[k].x);
-                        const uint4 w = __ldg(w4 + k);
-                        const uint4 vy = ld4(v, y, g.N, t.lane0);
+                    for (int e = 0; e < 2; e++) {
+                        const uint4& a = e ? a1 : a0;
 #pragma unroll
                         for (int j = 0; j < R; j++)
 #pragma unroll
-                            for (int l = 0; l < 4; l++) hx[e][j][l] = add(hx[e][j][l], mul(comp(vy, l), comp(w, j)));
+                            for (int l = 0; l < 4; l++) hx[e][j][l] = comp(a, j);
+                        for (uint32_t k = off[2 * s + e]; k < off[2 * s + e + 1]; k++) {
+                            const uint32_t y = __ldg(&mx_g[k].x);
+                            const uint4 w = __ldg(w4 + k);
+                            const uint4 vy = ld4(v, y, g.N, t.lane0);
+#pragma unroll
+                            for (int j = 0; j < R; j++)
+#pragma unroll
+                                for (int l = 0; l < 4; l++)
+                                    hx[e][j][l] = m31::mac_lazy(hx[e][j][l], comp(vy, l), comp(w, j));
+                        }
                     }
+#pragma unroll
+                    for (int j = 0; j < R; j++)
+#pragma unroll
+                        for (int l = 0; l < 4; l++)
+                            h[j][l] = fold(m31::from_u32(hx[0][j][l]), m31::from_u32(hx[1][j][l]), p.r[j]);
                 }
-                const uint4 v0 = ld4(v, 4 * i + 2 * s, g.N, t.lane0), v1 = ld4(v, 4 * i + 2 * s + 1, g.N, t.lane0);
 #pragma unroll
                 for (int j = 0; j < R; j++) {
-                    const uint32_t r = p.r[j];
-                    uint32_t f[4], h[4];
+                    uint32_t f[4];
 #pragma unroll
-                    for (int l = 0; l < 4; l++) {
-                        f[l] = fold(comp(v0, l), comp(v1, l), r);
-                        h[l] = fold(hx[0][j][l], hx[1][j][l], r);
-                    }
+                    for (int l = 0; l < 4; l++) f[l] = fold(comp(v0, l), comp(v1, l), p.r[j]);
                     st4(p.fdst[j], 2 * i + s, g.N, t.lane0, mk4(f));
-                    st4(p.hdst[j], 2 * i + s, g.N, t.lane0, mk4(h));
+                    st4(p.hdst[j], 2 * i + s, g.N, t.lane0, mk4(h[j]));
 #pragma unroll
                     for (int l = 0; l < 4; l++) {
                         if (s == 0) {
-                            acc[3 * j][l] = add(acc[3 * j][l], mul(f[l], h[l]));
-                            f0[j][l] = f[l];
-                            h0[j][l] = h[l];
+                            acc[3 * j][l] = m31::mac_lazy(acc[3 * j][l], f[l], h[j][l]);
+                            fe[j][l] = f[l];
+                            he[j][l] = h[j][l];
                         } else {
-                            acc[3 * j + 1][l] = add(acc[3 * j + 1][l], mul(f[l], h[l]));
-                            acc[3 * j + 2][l] = add(acc[3 * j + 2][l], mul(add(f0[j][l], f[l]), add(h0[j][l], h[l])));
+                            acc[3 * j + 1][l] = m31::mac_lazy(acc[3 * j + 1][l], f[l], h[j][l]);
+                            acc[3 * j + 2][l] =
+                                m31::mac_lazy(m31::mac_lazy(acc[3 * j + 2][l], fe[j][l], h[j][l]), f[l], he[j][l]);
                         }
                     }
                 }
             }
         }
     }
-    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R});
+    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R, true});
 }
 
 // ---------------------------------------------------------------- fold + reduce round
