@@ -18,6 +18,8 @@
 // The per-repetition kernels (k_hg_round0, k_round) give each CTA one repetition j =
 // blockIdx.x % R: the R CTAs of a row chunk are adjacent in launch order, run together and
 // share the layer input through L2, while each thread keeps only one repetition's state.
+#include <atomic>
+
 #include "kernels.cuh"
 #include "m31.cuh"
 
@@ -352,6 +354,7 @@ __device__ __forceinline__ void cp_async_wait() {
 // iterations ahead.
 constexpr int kStages = 3;
 constexpr int kStageFields = 5;  // v(2i), v(2i+1), a(2i), a(2i+1), (off(2i), off(2i+1), off(2i+2))
+constexpr int kMaxStagedSmem = kStages * kStageFields * 16 * 256;
 
 template <int R>
 __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict__ v, uint64_t I,
@@ -847,12 +850,21 @@ cudaError_t launch_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* 
 
 // Dynamic shared memory of the staged kernels: the cp.async ring, or the reduction's
 // scratch where that is larger (they share the allocation).
-template <class K>
-static size_t staged_smem(K kernel, size_t ring_bytes, size_t red_bytes) {
-    const size_t bytes = ring_bytes > red_bytes ? ring_bytes : red_bytes;
-    // above 48 KiB less the kernel's static shared memory the launch needs the opt-in
-    if (bytes > 40 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    return bytes;
+// Dynamic shared memory of k_hg_round0: the cp.async ring, or the reduction's scratch where
+// that is larger (they share the allocation).  Above 48 KiB less the kernel's static shared
+// memory a launch needs the opt-in, which is set once per device and instantiation to the
+// largest size any launch asks for (block <= 256).
+template <int R>
+static size_t hg0_smem(size_t ring_bytes, size_t red_bytes) {
+    static std::atomic<uint64_t> opted{0};  // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(opted.load(std::memory_order_relaxed) & bit)) {
+        cudaFuncSetAttribute(k_hg_round0<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxStagedSmem);
+        opted.fetch_or(bit);
+    }
+    return ring_bytes > red_bytes ? ring_bytes : red_bytes;
 }
 
 cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint32_t* mx_off, const uint4* mx_g,
@@ -867,7 +879,7 @@ cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint
     LaunchShape sh = row_shape(gb, I / 2, block, ctas, 3 * reps);
     const size_t ring = (size_t)kStages * kStageFields * sizeof(uint4) * block;
 #define GKR_HG0(RR)                                                                                          \
-    k_hg_round0<RR><<<sh.grid, sh.block, staged_smem(k_hg_round0<RR>, ring, sh.smem), s>>>(v, I, mx_off, mx_g, a4, \
+    k_hg_round0<RR><<<sh.grid, sh.block, hg0_smem<RR>(ring, sh.smem), s>>>(v, I, mx_off, mx_g, a4, \
                                                                                       w4, gb, red, evals_out)
     switch (reps) {
         case 1: GKR_HG0(1); break;
