@@ -672,64 +672,101 @@ __global__ void __launch_bounds__(256) k_round_shared(RoundPtrs p, uint64_t npai
     reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, LANE_HG ? nullptr : vx, g.N, (uint32_t)R});
 }
 
+// x == x mod p with x < 2^34: x = hi 2^32 + lo and 2^32 == 2 (mod 2^31 - 1), so
+// lo + 2 hi < 3 * 2^32; two multiply-adds on the integer FMA pipe (lo + 2 hi with its carry,
+// then bit 31 of hi plus that carry).  After it, three more products <= (p - 1)^2 keep a
+// 64-bit sum below 2^34 + 3 * 2^62.
+__device__ __forceinline__ uint64_t fold64(uint64_t x) {
+    uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32), nl, nh;
+    asm("mad.lo.cc.u32 %0, %2, 2, %3;\n\t"
+        "madc.hi.u32 %1, %2, 2, 0;"
+        : "=r"(nl), "=r"(nh)
+        : "r"(hi), "r"(lo));
+    return ((uint64_t)nh << 32) | nl;
+}
+
 // Phase-two round 0 (no fold): p0_j = sum f(2i) s_j(2i), p1_j = sum f(2i+1) s_j(2i+1),
-// p2raw_j = sum (f(2i) + f(2i+1)) (s_j(2i) + s_j(2i+1)) over the layer input f = v.  Three
-// products per pair, repetition and lane against 32 bytes read make this round bound by
-// integer instructions rather than HBM, so: one repetition per CTA (j = blockIdx.x % R,
-// the R CTAs of a row chunk adjacent so the rows come from L2 after the first read) for
-// light threads and high occupancy, and products summed unreduced in 64-bit accumulators,
-// folded mod p every third pair instead of fully reduced one by one.  Same results as
-// k_round_shared<R, false, false>.
-__global__ void __launch_bounds__(256) k_p2_round0(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx,
-                                                   Geo g, uint32_t reps, RedScratch red, uint32_t* evals_out) {
+// p2raw_j = sum (f(2i) + f(2i+1)) (s_j(2i) + s_j(2i+1)) over the layer input f = v, for
+// all R repetitions in one thread so that each row read serves the R scalar tables.  With
+// 4 bytes read per copy and row, the products are summed unreduced in 64-bit accumulators
+// (one multiply-add each, every factor canonical) and folded every third pair.  The pair's
+// two rows and the R scalar pairs are staged by cp.async kP2Stages - 1 iterations ahead.
+// Same results as k_round_shared<R, false, false>.
+constexpr int kP2Stages = 4;
+constexpr int kP2Fields = 4;  // v(2i), v(2i+1), (s_0, s_1) pairs, (s_2 pair, unused)
+constexpr int kMaxP2Smem = kP2Stages * kP2Fields * 16 * 256;
+
+template <int R>
+__global__ void __launch_bounds__(256, 2) k_p2_round0(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx,
+                                                      Geo g, RedScratch red, uint32_t* evals_out) {
+    extern __shared__ uint4 ring[];  // kP2Stages x kP2Fields x blockDim.x
     const TileIdx t = tile_idx(g);
-    const uint32_t j = blockIdx.x % reps, cx = blockIdx.x / reps, nx = gridDim.x / reps;
+    const uint32_t B = blockDim.x, tid = threadIdx.x;
     const uint32_t* __restrict__ fs = p.fsrc[0];
-    const uint2* __restrict__ sj =
-        reinterpret_cast<const uint2*>(j == 0 ? p.hsrc[0] : (j == 1 ? p.hsrc[1] : p.hsrc[2]));
-    uint64_t acc[3][4] = {};
-    auto pair = [&](const uint4& a0, const uint4& a1, const uint2& s) {
-        const uint32_t s01 = add(s.x, s.y);
+    uint64_t acc[3 * R][4];
 #pragma unroll
-        for (int l = 0; l < 4; l++) {
-            acc[0][l] += (uint64_t)comp(a0, l) * s.x;
-            acc[1][l] += (uint64_t)comp(a1, l) * s.y;
-            acc[2][l] += (uint64_t)add(comp(a0, l), comp(a1, l)) * s01;
-        }
-    };
-    // each product is < 2^62: after a fold (< 2^34) three more keep the sum < 2^64
-    auto fold_acc = [&]() {
+    for (int c = 0; c < 3 * R; c++)
 #pragma unroll
-        for (int c = 0; c < 3; c++)
-#pragma unroll
-            for (int l = 0; l < 4; l++) acc[c][l] = (acc[c][l] & m31::P) + (acc[c][l] >> 31);
-    };
+        for (int l = 0; l < 4; l++) acc[c][l] = 0ull;
     if (t.active) {
-        const uint64_t step = (uint64_t)nx * g.rps;
-        uint64_t i = (uint64_t)cx * g.rps + t.rs;
-        // three pairs per iteration: their six row loads are in flight together
-        for (; i + 2 * step < npairs; i += 3 * step) {
-            const uint64_t i1 = i + step, i2 = i + 2 * step;
-            const uint4 a0 = ld4(fs, 2 * i, g.N, t.lane0), a1 = ld4(fs, 2 * i + 1, g.N, t.lane0);
-            const uint4 b0 = ld4(fs, 2 * i1, g.N, t.lane0), b1 = ld4(fs, 2 * i1 + 1, g.N, t.lane0);
-            const uint4 c0 = ld4(fs, 2 * i2, g.N, t.lane0), c1 = ld4(fs, 2 * i2 + 1, g.N, t.lane0);
-            const uint2 sa = __ldg(sj + i), sb = __ldg(sj + i1), sc = __ldg(sj + i2);
-            pair(a0, a1, sa);
-            pair(b0, b1, sb);
-            pair(c0, c1, sc);
-            fold_acc();
-        }
-        for (; i < npairs; i += step) {
-            pair(ld4(fs, 2 * i, g.N, t.lane0), ld4(fs, 2 * i + 1, g.N, t.lane0), __ldg(sj + i));
-            fold_acc();
-        }
-    }
-    uint32_t out[3][4];
+        const uint64_t step = (uint64_t)gridDim.x * g.rps;
+        const uint64_t i0 = (uint64_t)blockIdx.x * g.rps + t.rs;
+        auto stage = [&](uint64_t i, int slot) {
+            if (i < npairs) {
+                uint4* st = ring + (size_t)slot * kP2Fields * B + tid;
+                cp_async16(st, fs + (2 * i) * g.N + t.lane0);
+                cp_async16(st + B, fs + (2 * i + 1) * g.N + t.lane0);
 #pragma unroll
-    for (int c = 0; c < 3; c++)
+                for (int j = 0; j < R; j++)
+                    cp_async8(reinterpret_cast<uint2*>(st + (2 + j / 2) * B) + (j & 1), p.hsrc[j] + 2 * i);
+            }
+            cp_async_commit();  // one group per iteration, empty past the end
+        };
+#pragma unroll
+        for (int s = 0; s < kP2Stages - 1; s++) stage(i0 + s * step, s);
+        int slot = 0;
+        uint32_t since_fold = 0;
+        for (uint64_t i = i0; i < npairs; i += step) {
+            stage(i + (kP2Stages - 1) * step, slot == 0 ? kP2Stages - 1 : slot - 1);
+            cp_async_wait<kP2Stages - 1>();
+            const uint4* st = ring + (size_t)slot * kP2Fields * B + tid;
+            const uint4 f0 = st[0], f1 = st[B];
+            uint32_t sa[R], sb[R], sab[R];
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                const uint2 sj = reinterpret_cast<const uint2*>(st + (2 + j / 2) * B)[j & 1];
+                sa[j] = sj.x;
+                sb[j] = sj.y;
+                sab[j] = add(sj.x, sj.y);
+            }
+#pragma unroll
+            for (int l = 0; l < 4; l++) {
+                const uint32_t a = comp(f0, l), b = comp(f1, l), ab = add(a, b);
+#pragma unroll
+                for (int j = 0; j < R; j++) {
+                    acc[3 * j][l] += (uint64_t)a * sa[j];
+                    acc[3 * j + 1][l] += (uint64_t)b * sb[j];
+                    acc[3 * j + 2][l] += (uint64_t)ab * sab[j];
+                }
+            }
+            if (++since_fold == 3) {
+                since_fold = 0;
+#pragma unroll
+                for (int c = 0; c < 3 * R; c++)
+#pragma unroll
+                    for (int l = 0; l < 4; l++) acc[c][l] = fold64(acc[c][l]);
+            }
+            slot = slot + 1 == kP2Stages ? 0 : slot + 1;
+        }
+        cp_async_wait<0>();
+    }
+    uint32_t out[3 * R][4];
+#pragma unroll
+    for (int c = 0; c < 3 * R; c++)
 #pragma unroll
         for (int l = 0; l < 4; l++) out[c][l] = reduce64(acc[c][l]);
-    reduce_group<3>(out, g, t.active, red, 3 * j, RoundFin{red, evals_out, vx, g.N, reps});
+    __syncthreads();  // the ring is reused as the reduction's scratch
+    reduce_group<3 * R>(out, g, t.active, red, 0, RoundFin{red, evals_out, vx, g.N, (uint32_t)R});
 }
 
 // ---------------------------------------------------------------- phase two: s(y)
@@ -904,6 +941,20 @@ cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const
     return cudaGetLastError();
 }
 
+// Shared-memory opt-in of k_p2_round0 (as hg0_smem): once per device and instantiation.
+template <int R>
+static size_t p2_smem(size_t bytes) {
+    static std::atomic<uint64_t> opted{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(opted.load(std::memory_order_relaxed) & bit)) {
+        cudaFuncSetAttribute(k_p2_round0<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxP2Smem);
+        opted.fetch_or(bit);
+    }
+    return bytes;
+}
+
 cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, const RoundPtrs& p, uint64_t npairs,
                          const uint32_t* vx, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
                          uint32_t* evals_out, cudaStream_t s) {
@@ -911,9 +962,20 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, co
     if (lane_hg && !fold_) return cudaErrorInvalidValue;  // phase-one round 0 lives in k_hg_round0
     if (!fold_ && !shared_src) return cudaErrorInvalidValue;
     if (!fold_) {
-        // phase-two round 0: integer-bound, one repetition per CTA (k_p2_round0)
-        LaunchShape sh = rep_shape(g, npairs, block, ctas, reps);
-        k_p2_round0<<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, (uint32_t)reps, red, evals_out);
+        // phase-two round 0 (k_p2_round0): launch bound 256 threads, wider tiles narrowed
+        Geo gb = g;
+        uint32_t b = block > 256 ? 256 : block;
+        while (gb.tpr > b && gb.tpr % 2 == 0) gb.tpr /= 2;
+        if (gb.tpr > b) return cudaErrorInvalidValue;
+        gb.rps = b / gb.tpr;
+        const LaunchShape sh = row_shape(gb, npairs, b, ctas, 3 * reps);
+        const size_t ring = (size_t)kP2Stages * kP2Fields * sizeof(uint4) * b;
+        const size_t smem = ring > sh.smem ? ring : sh.smem;
+        switch (reps) {
+            case 1: k_p2_round0<1><<<sh.grid, sh.block, p2_smem<1>(smem), s>>>(p, npairs, vx, gb, red, evals_out); break;
+            case 2: k_p2_round0<2><<<sh.grid, sh.block, p2_smem<2>(smem), s>>>(p, npairs, vx, gb, red, evals_out); break;
+            default: k_p2_round0<3><<<sh.grid, sh.block, p2_smem<3>(smem), s>>>(p, npairs, vx, gb, red, evals_out); break;
+        }
         return cudaGetLastError();
     }
     if (shared_src) {
