@@ -692,7 +692,7 @@ __device__ __forceinline__ uint64_t fold64(uint64_t x) {
 // (one multiply-add each, every factor canonical) and folded every third pair.  The pair's
 // two rows and the R scalar pairs are staged by cp.async kP2Stages - 1 iterations ahead.
 // Same results as k_round_shared<R, false, false>.
-constexpr int kP2Stages = 4;
+constexpr int kP2Stages = 6;
 constexpr int kP2Fields = 4;  // v(2i), v(2i+1), (s_0, s_1) pairs, (s_2 pair, unused)
 constexpr int kMaxP2Smem = kP2Stages * kP2Fields * 16 * 256;
 
