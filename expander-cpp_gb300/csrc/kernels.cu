@@ -552,7 +552,39 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, con
     const uint32_t r = j == 0 ? p.r[0] : (j == 1 ? p.r[1] : p.r[2]);
     uint32_t acc[3][4] = {};
     if (t.active) {
-        for (uint64_t i = (uint64_t)cx * g.rps + t.rs; i < npairs; i += (uint64_t)nx * g.rps) {
+        uint64_t i = (uint64_t)cx * g.rps + t.rs;
+        const uint64_t step = (uint64_t)nx * g.rps;
+        if (FOLD && !LANE_HG) {
+            // scalar-h folds: two pairs per iteration, their eight row loads issued together
+            auto fold_pair = [&](const uint4 (&a)[4], const uint4& sv, uint64_t ii) {
+                const uint32_t s0 = fold(sv.x, sv.y, r), s1 = fold(sv.z, sv.w, r);
+                if (t.q == 0 && blockIdx.y == 0) *reinterpret_cast<uint2*>(hd + 2 * ii) = make_uint2(s0, s1);
+                uint32_t f0[4], f1[4], h0[4], h1[4];
+#pragma unroll
+                for (int l = 0; l < 4; l++) {
+                    f0[l] = fold(comp(a[0], l), comp(a[1], l), r);
+                    f1[l] = fold(comp(a[2], l), comp(a[3], l), r);
+                    h0[l] = s0;
+                    h1[l] = s1;
+                }
+                st4(fd, 2 * ii, g.N, t.lane0, mk4(f0));
+                st4(fd, 2 * ii + 1, g.N, t.lane0, mk4(f1));
+                accum_pair(acc, f0, f1, h0, h1);
+            };
+            for (; i + step < npairs; i += 2 * step) {
+                uint4 a[4], b[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    a[k] = ld4(fs, 4 * i + k, g.N, t.lane0);
+                    b[k] = ld4(fs, 4 * (i + step) + k, g.N, t.lane0);
+                }
+                const uint4 sa = __ldg(reinterpret_cast<const uint4*>(hs) + i);
+                const uint4 sb = __ldg(reinterpret_cast<const uint4*>(hs) + i + step);
+                fold_pair(a, sa, i);
+                fold_pair(b, sb, i + step);
+            }
+        }
+        for (; i < npairs; i += step) {
             uint32_t f0[4], f1[4], h0[4], h1[4];
             if (FOLD) {
                 uint4 a[4];
