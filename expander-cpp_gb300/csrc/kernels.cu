@@ -511,7 +511,8 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
 #pragma unroll
                     for (int l = 0; l < 4; l++) f[l] = fold(comp(v0, l), comp(v1, l), p.r[j]);
                     st4(p.fdst[j], 2 * i + s, g.N, t.lane0, mk4(f));
-                    st4(p.hdst[j], 2 * i + s, g.N, t.lane0, mk4(h[j]));
+                    // a copy-independent hg row is recomputed by round 2 (k_round with H1)
+                    if (off[2 * s] != off[2 * s + 2]) st4(p.hdst[j], 2 * i + s, g.N, t.lane0, mk4(h[j]));
 #pragma unroll
                     for (int l = 0; l < 4; l++) {
                         if (s == 0) {
@@ -539,7 +540,9 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
 // SHARED: every repetition folds the same source table (the layer input at round 1).
 // LANE_HG: hg is a per-copy table (phase one); otherwise it is a copy-independent scalar
 // table s_j (phase two) and the finisher multiplies the sums by vx_j.
-template <bool SHARED, bool LANE_HG, bool FOLD>
+// H1 (phase-one round 2): source hg row q whose input rows 2q, 2q+1 have no mul gates was
+// not stored by k_hg_round1 and is recomputed as fold(a_j(2q), a_j(2q+1), r0_j).
+template <bool SHARED, bool LANE_HG, bool FOLD, bool H1 = false>
 __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx, Geo g,
                                                uint32_t reps, RedScratch red, uint32_t* evals_out) {
     const TileIdx t = tile_idx(g);
@@ -592,8 +595,25 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, con
                 for (int k = 0; k < 4; k++) a[k] = ld4(fs, 4 * i + k, g.N, t.lane0);
                 if (LANE_HG) {
                     uint4 b[4];
+                    if (H1) {
+                        const uint4 oa = __ldg(reinterpret_cast<const uint4*>(p.hoff + 8 * i));
+                        const uint4 ob = __ldg(reinterpret_cast<const uint4*>(p.hoff + 8 * i + 4));
+                        const uint32_t off[9] = {oa.x, oa.y, oa.z, oa.w, ob.x, ob.y, ob.z, ob.w, __ldg(p.hoff + 8 * i + 8)};
+                        const uint32_t hr = j == 0 ? p.hr[0] : (j == 1 ? p.hr[1] : p.hr[2]);
 #pragma unroll
-                    for (int k = 0; k < 4; k++) b[k] = ld4(hs, 4 * i + k, g.N, t.lane0);
+                        for (int k = 0; k < 4; k++) {
+                            if (off[2 * k] == off[2 * k + 2]) {
+                                const uint32_t* a = reinterpret_cast<const uint32_t*>(p.ha + 8 * i + 2 * k) + j;
+                                const uint32_t hv = fold(__ldg(a), __ldg(a + 4), hr);
+                                b[k] = make_uint4(hv, hv, hv, hv);
+                            } else {
+                                b[k] = ld4(hs, 4 * i + k, g.N, t.lane0);
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < 4; k++) b[k] = ld4(hs, 4 * i + k, g.N, t.lane0);
+                    }
 #pragma unroll
                     for (int l = 0; l < 4; l++) {
                         h0[l] = fold(comp(b[0], l), comp(b[1], l), r);
@@ -728,13 +748,21 @@ constexpr int kP2Stages = 6;
 constexpr int kP2Fields = 4;  // v(2i), v(2i+1), (s_0, s_1) pairs, (s_2 pair, unused)
 constexpr int kMaxP2Smem = kP2Stages * kP2Fields * 16 * 256;
 
+struct P2Src {
+    const uint32_t* f;     // the layer input, 2 npairs rows
+    const uint32_t* s[3];  // the repetitions' scalar tables s_j
+};
+
 template <int R>
-__global__ void __launch_bounds__(256, 2) k_p2_round0(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx,
+__global__ void __launch_bounds__(256, 2) k_p2_round0(P2Src src, uint64_t npairs, const uint32_t* __restrict__ vx,
                                                       Geo g, RedScratch red, uint32_t* evals_out) {
     extern __shared__ uint4 ring[];  // kP2Stages x kP2Fields x blockDim.x
     const TileIdx t = tile_idx(g);
     const uint32_t B = blockDim.x, tid = threadIdx.x;
-    const uint32_t* __restrict__ fs = p.fsrc[0];
+    const uint32_t* __restrict__ fs = src.f;
+    const uint32_t* hsrc[R];
+#pragma unroll
+    for (int j = 0; j < R; j++) hsrc[j] = src.s[j];
     uint64_t acc[3 * R][4];
 #pragma unroll
     for (int c = 0; c < 3 * R; c++)
@@ -750,7 +778,7 @@ __global__ void __launch_bounds__(256, 2) k_p2_round0(RoundPtrs p, uint64_t npai
                 cp_async16(st + B, fs + (2 * i + 1) * g.N + t.lane0);
 #pragma unroll
                 for (int j = 0; j < R; j++)
-                    cp_async8(reinterpret_cast<uint2*>(st + (2 + j / 2) * B) + (j & 1), p.hsrc[j] + 2 * i);
+                    cp_async8(reinterpret_cast<uint2*>(st + (2 + j / 2) * B) + (j & 1), hsrc[j] + 2 * i);
             }
             cp_async_commit();  // one group per iteration, empty past the end
         };
@@ -1003,10 +1031,11 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, co
         const LaunchShape sh = row_shape(gb, npairs, b, ctas, 3 * reps);
         const size_t ring = (size_t)kP2Stages * kP2Fields * sizeof(uint4) * b;
         const size_t smem = ring > sh.smem ? ring : sh.smem;
+        const P2Src src{p.fsrc[0], {p.hsrc[0], p.hsrc[1], p.hsrc[2]}};
         switch (reps) {
-            case 1: k_p2_round0<1><<<sh.grid, sh.block, p2_smem<1>(smem), s>>>(p, npairs, vx, gb, red, evals_out); break;
-            case 2: k_p2_round0<2><<<sh.grid, sh.block, p2_smem<2>(smem), s>>>(p, npairs, vx, gb, red, evals_out); break;
-            default: k_p2_round0<3><<<sh.grid, sh.block, p2_smem<3>(smem), s>>>(p, npairs, vx, gb, red, evals_out); break;
+            case 1: k_p2_round0<1><<<sh.grid, sh.block, p2_smem<1>(smem), s>>>(src, npairs, vx, gb, red, evals_out); break;
+            case 2: k_p2_round0<2><<<sh.grid, sh.block, p2_smem<2>(smem), s>>>(src, npairs, vx, gb, red, evals_out); break;
+            default: k_p2_round0<3><<<sh.grid, sh.block, p2_smem<3>(smem), s>>>(src, npairs, vx, gb, red, evals_out); break;
         }
         return cudaGetLastError();
     }
@@ -1036,6 +1065,14 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, co
         else GKR_ROUND(false, false, true);
     }
 #undef GKR_ROUND
+    return cudaGetLastError();
+}
+
+cudaError_t launch_round_h1(int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
+                            uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
+    if (reps < 1 || reps > 3 || !p.hoff || !p.ha) return cudaErrorInvalidValue;
+    LaunchShape sh = rep_shape(g, npairs, block, ctas, reps);
+    k_round<false, true, true, true><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
     return cudaGetLastError();
 }
 

@@ -164,6 +164,9 @@ struct DevLayer {
     // phase two: mul gates grouped by y = i1
     uint32_t* my_off = nullptr;  // I+1
     uint4* my_g = nullptr;       // (x, z, c, 0)
+    // phase-one rows q < I/2 after round 0 whose input rows 2q, 2q+1 have no mul gates: their
+    // hg is the same for every copy, is not stored by round 1 and is recomputed in round 2
+    uint64_t h1_scalar_rows = 0;
     // BN254 circuits: each gate's coefficient in Montgomery form, in the order of the table above
     const bn::Fr *mo_c = nullptr, *ao_c = nullptr, *mx_c = nullptr, *ax_c = nullptr, *my_c = nullptr;
     void* block = nullptr;
@@ -512,6 +515,8 @@ DevLayer upload_layer(const gkrgpu_layer_desc& d, int field) {
     }
     for (uint64_t i = 0; i < Gm; i++) keys[i] = d.mul[i].i0;
     csr(I, Gm, keys, off_mx, ord);
+    uint64_t h1_scalar = 0;
+    for (uint64_t q = 0; q < I / 2; q++) h1_scalar += off_mx[2 * q] == off_mx[2 * q + 2];
     for (uint64_t k = 0; k < Gm; k++) {
         const auto& g = d.mul[ord[k]];
         mx[k] = make_uint4(g.i1, g.o_id, g.coef, 0);
@@ -546,6 +551,7 @@ DevLayer upload_layer(const gkrgpu_layer_desc& d, int field) {
         void** dst;
     };
     DevLayer L;
+    L.h1_scalar_rows = h1_scalar;
     L.nin = d.nb_input_vars;
     L.nout = d.nb_output_vars;
     L.nmul = Gm;
@@ -857,9 +863,20 @@ struct Prover {
             if (k == 1) {
                 // hg rebuilt from the weights: v read once, the gathers again, f and hg halves out
                 kid = K_HG_ROUND1;
-                c.launch(K_HG_ROUND1, rb * (I + Ly.nmul + (double)R * I) + 32.0 * Ly.nmul + 20.0 * I, [&] {
+                c.launch(K_HG_ROUND1, rb * (I + Ly.nmul + (double)R * I - (double)R * Ly.h1_scalar_rows) + 32.0 * Ly.nmul + 20.0 * I, [&] {
                     return launch_hg_round1(R, v, npairs, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, p, gk[K_HG_ROUND1],
                                             X.block, ck_ctas[K_HG_ROUND1], red_mapped(), c.evals_d(), c.stream);
+                });
+            } else if (k == 2) {
+                // round-1 hg rows of input pairs without mul gates were not stored: recomputed
+                // from the add weights at the round-0 challenges
+                p.hoff = Ly.mx_off;
+                p.ha = ws.a4;
+                for (int j = 0; j < R; j++) p.hr[j] = rx[j][0];
+                const double hsc = (double)R * Ly.h1_scalar_rows;
+                c.launch(K_ROUND_LANE, rb * (3.0 * R * S - hsc) + hsc * 32.0 + 36.0 * npairs * R, [&] {
+                    return launch_round_h1(R, p, npairs, gk[K_ROUND_LANE], X.block, ck_ctas[K_ROUND_LANE], red_mapped(),
+                                           c.evals_d(), c.stream);
                 });
             } else {
                 c.launch(K_ROUND_LANE, rb * 3.0 * R * S, [&] {
