@@ -540,9 +540,11 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
 // SHARED: every repetition folds the same source table (the layer input at round 1).
 // LANE_HG: hg is a per-copy table (phase one); otherwise it is a copy-independent scalar
 // table s_j (phase two) and the finisher multiplies the sums by vx_j.
-// H1 (phase-one round 2): source hg row q whose input rows 2q, 2q+1 have no mul gates was
-// not stored by k_hg_round1 and is recomputed as fold(a_j(2q), a_j(2q+1), r0_j).
-template <bool SHARED, bool LANE_HG, bool FOLD, bool H1 = false>
+// HR (phase-one rounds 2 and 3, HR = round - 1): a source hg row q covers the 2^HR input
+// rows q 2^HR .. (q+1) 2^HR - 1; where none of them has mul gates the previous round did
+// not store it, and it is recomputed by folding their add weights a_j at the challenges of
+// rounds 0 .. HR-1.  Round 2 (HR = 1) does not store its own output rows of that kind.
+template <bool SHARED, bool LANE_HG, bool FOLD, int HR = 0>
 __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx, Geo g,
                                                uint32_t reps, RedScratch red, uint32_t* evals_out) {
     const TileIdx t = tile_idx(g);
@@ -595,20 +597,30 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, con
                 for (int k = 0; k < 4; k++) a[k] = ld4(fs, 4 * i + k, g.N, t.lane0);
                 if (LANE_HG) {
                     uint4 b[4];
-                    if (H1) {
-                        const uint4 oa = __ldg(reinterpret_cast<const uint4*>(p.hoff + 8 * i));
-                        const uint4 ob = __ldg(reinterpret_cast<const uint4*>(p.hoff + 8 * i + 4));
-                        const uint32_t off[9] = {oa.x, oa.y, oa.z, oa.w, ob.x, ob.y, ob.z, ob.w, __ldg(p.hoff + 8 * i + 8)};
-                        const uint32_t hr = j == 0 ? p.hr[0] : (j == 1 ? p.hr[1] : p.hr[2]);
+                    bool keep0 = true, keep1 = true;  // store output rows 2i, 2i+1
+                    if (HR > 0) {
+                        constexpr int SPAN = 1 << HR;  // input rows per source row
+                        // offsets of input rows 4i SPAN .. 4(i+1) SPAN at the source rows' ends
+                        uint32_t off[5];
+                        const uint32_t* o = p.hoff + 4 * SPAN * i;
+#pragma unroll
+                        for (int k = 0; k <= 4; k++) off[k] = __ldg(o + k * SPAN);
+                        const uint32_t r0 = j == 0 ? p.hr[0][0] : (j == 1 ? p.hr[0][1] : p.hr[0][2]);
+                        const uint32_t r1 = j == 0 ? p.hr[1][0] : (j == 1 ? p.hr[1][1] : p.hr[1][2]);
 #pragma unroll
                         for (int k = 0; k < 4; k++) {
-                            if (off[2 * k] == off[2 * k + 2]) {
-                                const uint32_t* a = reinterpret_cast<const uint32_t*>(p.ha + 8 * i + 2 * k) + j;
-                                const uint32_t hv = fold(__ldg(a), __ldg(a + 4), hr);
+                            if (off[k] == off[k + 1]) {
+                                const uint32_t* a = reinterpret_cast<const uint32_t*>(p.ha + (4 * i + k) * SPAN) + j;
+                                uint32_t hv = fold(__ldg(a), __ldg(a + 4), r0);
+                                if (HR == 2) hv = fold(hv, fold(__ldg(a + 8), __ldg(a + 12), r0), r1);
                                 b[k] = make_uint4(hv, hv, hv, hv);
                             } else {
                                 b[k] = ld4(hs, 4 * i + k, g.N, t.lane0);
                             }
+                        }
+                        if (HR == 1) {
+                            keep0 = off[0] != off[2];
+                            keep1 = off[2] != off[4];
                         }
                     } else {
 #pragma unroll
@@ -619,8 +631,8 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, con
                         h0[l] = fold(comp(b[0], l), comp(b[1], l), r);
                         h1[l] = fold(comp(b[2], l), comp(b[3], l), r);
                     }
-                    st4(hd, 2 * i, g.N, t.lane0, mk4(h0));
-                    st4(hd, 2 * i + 1, g.N, t.lane0, mk4(h1));
+                    if (keep0) st4(hd, 2 * i, g.N, t.lane0, mk4(h0));
+                    if (keep1) st4(hd, 2 * i + 1, g.N, t.lane0, mk4(h1));
                 } else {
                     const uint4 s = __ldg(reinterpret_cast<const uint4*>(hs) + i);
                     const uint32_t s0 = fold(s.x, s.y, r), s1 = fold(s.z, s.w, r);
@@ -1068,11 +1080,14 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, co
     return cudaGetLastError();
 }
 
-cudaError_t launch_round_h1(int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
+cudaError_t launch_round_hr(int round, int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
-    if (reps < 1 || reps > 3 || !p.hoff || !p.ha) return cudaErrorInvalidValue;
+    if (reps < 1 || reps > 3 || !p.hoff || !p.ha || (round != 2 && round != 3)) return cudaErrorInvalidValue;
     LaunchShape sh = rep_shape(g, npairs, block, ctas, reps);
-    k_round<false, true, true, true><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
+    if (round == 2)
+        k_round<false, true, true, 1><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
+    else
+        k_round<false, true, true, 2><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
     return cudaGetLastError();
 }
 

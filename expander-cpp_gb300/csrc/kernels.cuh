@@ -39,12 +39,13 @@ struct RoundPtrs {
     const uint32_t* hsrc[3];
     uint32_t* hdst[3];
     uint32_t r[3];
-    // Phase-one round 2 only: the round-1 hg rows whose two input rows have no mul gates
-    // were not stored; they are fold(a_j(2q), a_j(2q+1), r0_j) from the layer's CSR offsets
-    // by input row (hoff), add weights (ha) and round-0 challenges (hr).
+    // Phase-one rounds 2 and 3: the stored hg rows of the previous round whose input rows
+    // (2 or 4 of them) have no mul gates were not stored; they are the folds of the add
+    // weights a_j of those rows at the earlier challenges, from the layer's CSR offsets by
+    // input row (hoff), add weights (ha) and the challenges of rounds 0 and 1 (hr[round][j]).
     const uint32_t* hoff;
     const uint4* ha;
-    uint32_t hr[3];
+    uint32_t hr[2][3];
 };
 
 struct LaunchShape {
@@ -112,9 +113,10 @@ cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint
 cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* mx_off, const uint4* mx_g,
                              const uint4* a4, const uint4* w4, const RoundPtrs& p, const Geo& g, uint32_t block,
                              uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
-// Phase-one round 2 (a k_round with per-copy hg and fold) reading the round-1 hg rows that
-// k_hg_round1 stored and recomputing the copy-independent ones (p.hoff, p.ha, p.hr).
-cudaError_t launch_round_h1(int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
+// Phase-one round 2 or 3 (k = round, a k_round with per-copy hg and fold) reading the
+// previous round's stored hg rows and recomputing the copy-independent ones (p.hoff, p.ha,
+// p.hr); round 2 in turn does not store its copy-independent output rows.
+cudaError_t launch_round_hr(int round, int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
 cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold, const RoundPtrs& p, uint64_t npairs,
                          const uint32_t* vx, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,

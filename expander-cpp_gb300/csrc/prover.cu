@@ -167,6 +167,9 @@ struct DevLayer {
     // phase-one rows q < I/2 after round 0 whose input rows 2q, 2q+1 have no mul gates: their
     // hg is the same for every copy, is not stored by round 1 and is recomputed in round 2
     uint64_t h1_scalar_rows = 0;
+    // the same after round 1: rows q < I/4 whose input rows 4q .. 4q+3 have no mul gates (not
+    // stored by round 2, recomputed in round 3)
+    uint64_t h2_scalar_rows = 0;
     // BN254 circuits: each gate's coefficient in Montgomery form, in the order of the table above
     const bn::Fr *mo_c = nullptr, *ao_c = nullptr, *mx_c = nullptr, *ax_c = nullptr, *my_c = nullptr;
     void* block = nullptr;
@@ -515,8 +518,9 @@ DevLayer upload_layer(const gkrgpu_layer_desc& d, int field) {
     }
     for (uint64_t i = 0; i < Gm; i++) keys[i] = d.mul[i].i0;
     csr(I, Gm, keys, off_mx, ord);
-    uint64_t h1_scalar = 0;
+    uint64_t h1_scalar = 0, h2_scalar = 0;
     for (uint64_t q = 0; q < I / 2; q++) h1_scalar += off_mx[2 * q] == off_mx[2 * q + 2];
+    for (uint64_t q = 0; q < I / 4; q++) h2_scalar += off_mx[4 * q] == off_mx[4 * q + 4];
     for (uint64_t k = 0; k < Gm; k++) {
         const auto& g = d.mul[ord[k]];
         mx[k] = make_uint4(g.i1, g.o_id, g.coef, 0);
@@ -552,6 +556,7 @@ DevLayer upload_layer(const gkrgpu_layer_desc& d, int field) {
     };
     DevLayer L;
     L.h1_scalar_rows = h1_scalar;
+    L.h2_scalar_rows = h2_scalar;
     L.nin = d.nb_input_vars;
     L.nout = d.nb_output_vars;
     L.nmul = Gm;
@@ -867,16 +872,23 @@ struct Prover {
                     return launch_hg_round1(R, v, npairs, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, p, gk[K_HG_ROUND1],
                                             X.block, ck_ctas[K_HG_ROUND1], red_mapped(), c.evals_d(), c.stream);
                 });
-            } else if (k == 2) {
-                // round-1 hg rows of input pairs without mul gates were not stored: recomputed
-                // from the add weights at the round-0 challenges
+            } else if (k == 2 || k == 3) {
+                // the previous round's hg rows whose input rows have no mul gates were not
+                // stored: recomputed from the add weights at the earlier challenges
                 p.hoff = Ly.mx_off;
                 p.ha = ws.a4;
-                for (int j = 0; j < R; j++) p.hr[j] = rx[j][0];
-                const double hsc = (double)R * Ly.h1_scalar_rows;
-                c.launch(K_ROUND_LANE, rb * (3.0 * R * S - hsc) + hsc * 32.0 + 36.0 * npairs * R, [&] {
-                    return launch_round_h1(R, p, npairs, gk[K_ROUND_LANE], X.block, ck_ctas[K_ROUND_LANE], red_mapped(),
-                                           c.evals_d(), c.stream);
+                for (int j = 0; j < R; j++) {
+                    p.hr[0][j] = rx[j][0];
+                    p.hr[1][j] = rx[j][1];
+                }
+                // rows not read (k = 2, 3) and not written (k = 2); a4 words and offsets instead
+                const double in_sc = (double)R * (k == 2 ? Ly.h1_scalar_rows : Ly.h2_scalar_rows);
+                const double out_sc = k == 2 ? (double)R * Ly.h2_scalar_rows : 0.0;
+                const double span = k == 2 ? 2.0 : 4.0;
+                const double hb2 = rb * (3.0 * R * S - in_sc - out_sc) + in_sc * 16.0 * span + 20.0 * npairs * R;
+                c.launch(K_ROUND_LANE, hb2, [&] {
+                    return launch_round_hr((int)k, R, p, npairs, gk[K_ROUND_LANE], X.block, ck_ctas[K_ROUND_LANE],
+                                           red_mapped(), c.evals_d(), c.stream);
                 });
             } else {
                 c.launch(K_ROUND_LANE, rb * 3.0 * R * S, [&] {
