@@ -755,7 +755,8 @@ __device__ __forceinline__ uint64_t fold64(uint64_t x) {
 // 4 bytes read per copy and row, the products are summed unreduced in 64-bit accumulators
 // (one multiply-add each, every factor canonical) and folded every third pair.  The pair's
 // two rows and the R scalar pairs are staged by cp.async kP2Stages - 1 iterations ahead.
-// Same results as k_round_shared<R, false, false>.
+// (SumcheckMultiLinearProdHelper::poly_eval_at on the first phase-two round,
+// sumcheck_helper.hpp:68-102, with hg = v(rx) s: the finisher multiplies by vx.)
 constexpr int kP2Stages = 6;
 constexpr int kP2Fields = 4;  // v(2i), v(2i+1), (s_0, s_1) pairs, (s_2 pair, unused)
 constexpr int kMaxP2Smem = kP2Stages * kP2Fields * 16 * 256;
