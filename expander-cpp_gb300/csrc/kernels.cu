@@ -696,8 +696,10 @@ __global__ void __launch_bounds__(256) k_round_shared(RoundPtrs p, uint64_t npai
                         f0[l] = fold(comp(a[0], l), comp(a[1], l), r);
                         f1[l] = fold(comp(a[2], l), comp(a[3], l), r);
                     }
-                    st4(p.fdst[j], 2 * i, g.N, t.lane0, mk4(f0));
-                    st4(p.fdst[j], 2 * i + 1, g.N, t.lane0, mk4(f1));
+                    if (p.fdst[j]) {  // null: the next round refolds the source instead
+                        st4(p.fdst[j], 2 * i, g.N, t.lane0, mk4(f0));
+                        st4(p.fdst[j], 2 * i + 1, g.N, t.lane0, mk4(f1));
+                    }
                 } else {
 #pragma unroll
                     for (int l = 0; l < 4; l++) { f0[l] = comp(a[0], l); f1[l] = comp(a[1], l); }
@@ -734,6 +736,52 @@ __global__ void __launch_bounds__(256) k_round_shared(RoundPtrs p, uint64_t npai
         }
     }
     reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, LANE_HG ? nullptr : vx, g.N, (uint32_t)R});
+}
+
+// Phase-two round 2 from the layer input: round 1 stored only its folded scalar tables, not
+// the folded copies f1_j(q) = fold(v(2q), v(2q+1), r0_j), which would be written once and
+// read once; here each output pair i refolds the eight input rows 8i..8i+7 at r0_j (p.hr[0])
+// and then at r1_j (p.r), stores rows 2i, 2i+1 of f2_j and the folded scalars, and sums the
+// round-2 evaluations (receive_challenge + poly_eval_at, sumcheck_helper.hpp:68-133).  All
+// repetitions in one thread: the eight rows are read once for the R tables.
+template <int R>
+__global__ void __launch_bounds__(256) k_p2_round2(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx,
+                                                   Geo g, RedScratch red, uint32_t* evals_out) {
+    const TileIdx t = tile_idx(g);
+    const uint32_t* __restrict__ fs = p.fsrc[0];
+    uint32_t acc[3 * R][4];
+#pragma unroll
+    for (int c = 0; c < 3 * R; c++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[c][l] = 0u;
+    if (t.active) {
+        for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
+            uint4 a[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) a[k] = ld4(fs, 8 * i + k, g.N, t.lane0);
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                const uint32_t r0 = p.hr[0][j], r1 = p.r[j];
+                const uint4 sv = __ldg(reinterpret_cast<const uint4*>(p.hsrc[j]) + i);
+                const uint32_t s0 = fold(sv.x, sv.y, r1), s1 = fold(sv.z, sv.w, r1);
+                if (t.q == 0 && blockIdx.y == 0) *reinterpret_cast<uint2*>(p.hdst[j] + 2 * i) = make_uint2(s0, s1);
+                uint32_t f0[4], f1[4], h0[4], h1[4];
+#pragma unroll
+                for (int l = 0; l < 4; l++) {
+                    const uint32_t g0 = fold(comp(a[0], l), comp(a[1], l), r0), g1 = fold(comp(a[2], l), comp(a[3], l), r0);
+                    const uint32_t g2 = fold(comp(a[4], l), comp(a[5], l), r0), g3 = fold(comp(a[6], l), comp(a[7], l), r0);
+                    f0[l] = fold(g0, g1, r1);
+                    f1[l] = fold(g2, g3, r1);
+                    h0[l] = s0;
+                    h1[l] = s1;
+                }
+                st4(p.fdst[j], 2 * i, g.N, t.lane0, mk4(f0));
+                st4(p.fdst[j], 2 * i + 1, g.N, t.lane0, mk4(f1));
+                accum_pair(*reinterpret_cast<uint32_t(*)[3][4]>(&acc[3 * j]), f0, f1, h0, h1);
+            }
+        }
+    }
+    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, vx, g.N, (uint32_t)R});
 }
 
 // x == x mod p with x < 2^34: x = hi 2^32 + lo and 2^32 == 2 (mod 2^31 - 1), so
@@ -1089,6 +1137,18 @@ cudaError_t launch_round_hr(int round, int reps, const RoundPtrs& p, uint64_t np
         k_round<false, true, true, 1><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
     else
         k_round<false, true, true, 2><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_p2_round2(int reps, const RoundPtrs& p, uint64_t npairs, const uint32_t* vx, const Geo& g,
+                             uint32_t block, uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
+    LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
+    switch (reps) {
+        case 1: k_p2_round2<1><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out); break;
+        case 2: k_p2_round2<2><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out); break;
+        case 3: k_p2_round2<3><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out); break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

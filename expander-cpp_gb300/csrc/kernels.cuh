@@ -118,6 +118,10 @@ cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const
 // p.hr); round 2 in turn does not store its copy-independent output rows.
 cudaError_t launch_round_hr(int round, int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
+// Phase-two round 2 refolding the layer input p.fsrc[0] at the round-0 challenges p.hr[0]
+// (round 1 stored only its scalar tables) and at p.r; outputs p.fdst / p.hdst as k_round.
+cudaError_t launch_p2_round2(int reps, const RoundPtrs& p, uint64_t npairs, const uint32_t* vx, const Geo& g,
+                             uint32_t block, uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
 cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold, const RoundPtrs& p, uint64_t npairs,
                          const uint32_t* vx, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
                          uint32_t* evals_out, cudaStream_t s);

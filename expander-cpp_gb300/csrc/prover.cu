@@ -939,11 +939,28 @@ struct Prover {
             }
             const uint64_t npairs = I >> (k + 1);
             const double S = 4.0 * npairs;
-            const double b = rb * ((k == 1 ? 1.0 : R) * S + R * S / 2) + 6.0 * R * S;
-            c.launch(K_ROUND_SCALAR, b, [&] {
-                return launch_round(R, k == 1, false, true, p, npairs, ws.vx, gk[K_ROUND_SCALAR], X.block,
-                                    ck_ctas[K_ROUND_SCALAR], red_mapped(), c.evals_d(), c.stream);
-            });
+            // with a round 2, round 1 stores only its scalar tables and round 2 refolds the
+            // layer input (the round-1 copies would be written once and read once)
+            const bool refold = n >= 3;
+            if (k == 1 && refold)
+                for (int j = 0; j < R; j++) p.fdst[j] = nullptr;
+            if (k == 2 && refold) {
+                for (int j = 0; j < R; j++) {
+                    p.fsrc[j] = v;
+                    p.hr[0][j] = ry[j][0];
+                }
+                const double b = rb * (2.0 * S + R * S / 2) + 6.0 * R * S;
+                c.launch(K_ROUND_SCALAR, b, [&] {
+                    return launch_p2_round2(R, p, npairs, ws.vx, gk[K_ROUND_SCALAR], X.block, ck_ctas[K_ROUND_SCALAR],
+                                            red_mapped(), c.evals_d(), c.stream);
+                });
+            } else {
+                const double b = rb * ((k == 1 ? 1.0 : R) * S + (k == 1 && refold ? 0.0 : R * S / 2)) + 6.0 * R * S;
+                c.launch(K_ROUND_SCALAR, b, [&] {
+                    return launch_round(R, k == 1, false, true, p, npairs, ws.vx, gk[K_ROUND_SCALAR], X.block,
+                                        ck_ctas[K_ROUND_SCALAR], red_mapped(), c.evals_d(), c.stream);
+                });
+            }
             const bool last = (k == n - 1);
             fetch(groups(K_ROUND_SCALAR), last ? p.fdst : nullptr, false);
             transcript_round(t, ry, k, last, false, vy.data());
