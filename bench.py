@@ -64,6 +64,9 @@ def parse():
                          "64 proofs batched")
     ap.add_argument("--proofs", type=int, default=512, help="mixed/serve: number of distinct proofs")
     ap.add_argument("--lanes", type=int, default=16, help="mixed/serve: proofs whose device stages overlap")
+    ap.add_argument("--plain-lanes", type=int, default=1,
+                    help="plain: proofs whose device stages overlap (one proof's per-round host round trips "
+                         "leave the device idle unless another proof's kernels fill them)")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="mixed/serve: device-memory admission budget")
     ap.add_argument("--rates", default="200,500,1000,2000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=4.0, help="serve: seconds of arrivals per rate")
@@ -286,6 +289,8 @@ def run_ours(args, D):
     circ, widths, cfg = workload(args)
     N = args.copies
     ctx = Context(device)
+    if args.plain_lanes > 1:
+        ctx.set_concurrency(lanes=args.plain_lanes)
     if args.tile:
         ctx.set_tile(*[int(x) for x in args.tile.split(",")])
     dc = ctx.load(circ)

@@ -58,6 +58,24 @@ def test_gpu_matches_oracle_random(ctx, oracle, seed, widths, n):
     assert np.array_equal(cv, ocv)
 
 
+@pytest.mark.parametrize("seed,widths,p_mul", [
+    (301, [14, 6, 14], 0.6),   # wide input layer: almost every input row without mul gates
+    (302, [12, 12, 12], 0.0),  # no mul gates: every phase-one hg row is copy-independent
+    (303, [10, 13, 10], 1.0),  # every input row of the first layer with mul gates
+    (304, [11, 9, 11, 9], 0.3),
+])
+def test_gpu_hg_rows_without_mul_gates(ctx, oracle, seed, widths, p_mul):
+    """Phase-one hg rows whose input rows have no mul gates are left unwritten by rounds 1
+    and 2 and recomputed from the add weights by rounds 2 and 3; mixes of such rows and
+    gated rows must give the oracle's proof."""
+    circ = gc.random_circuit(seed, widths, p_mul=p_mul, p_local=0.5, window=64)
+    w = gc.random_witness(seed, circ.log_input_size, 16)
+    cv, proof = ctx.prove(ctx.load(circ), w)
+    ocv, oproof = oracle.prove(circ, w)
+    assert proof == oproof
+    assert np.array_equal(cv, ocv)
+
+
 def test_gpu_proof_tamper_rejected(ctx, oracle):
     circ, w, grind = cases.build("cfg1_n16")
     cv, proof = ctx.prove(ctx.load(circ), w)
