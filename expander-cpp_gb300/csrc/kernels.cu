@@ -70,6 +70,9 @@ __device__ __forceinline__ uint32_t take(const RedScratch& red, uint32_t c, uint
 // row slices, one 64-bit atomic add per (component, lane) into red.acc at component
 // comp_base + c, then the last CTA of this lane group (ticket blockIdx.y) hands every lane
 // of the group to fin(lane), which collects the totals with take().
+template <class Fin>
+__device__ __forceinline__ void finish_group(const RedScratch& red, uint32_t base, uint32_t lanes, Fin& fin);
+
 template <int C, class Fin>
 __device__ __forceinline__ void reduce_group(const uint32_t (&acc)[C][4], const Geo& g, bool active, RedScratch red,
                                              uint32_t comp_base, Fin fin) {
@@ -90,6 +93,15 @@ __device__ __forceinline__ void reduce_group(const uint32_t (&acc)[C][4], const 
         const uint32_t lane = (blockIdx.y * tpr + q) * 4 + l;
         atomicAdd(&red.acc[(size_t)(comp_base + c) * g.N + lane], s);
     }
+    finish_group(red, blockIdx.y * 4 * tpr, 4 * tpr, fin);
+}
+
+// After a CTA's atomic adds: the last CTA of lane group blockIdx.y (ticket) hands lanes
+// base .. base + lanes - 1 to fin(lane), re-arms the ticket and, with red.done, publishes
+// the group's results to the host (system-scope fence, then the completion counter).
+template <class Fin>
+__device__ __forceinline__ void finish_group(const RedScratch& red, uint32_t base, uint32_t lanes, Fin& fin) {
+    const uint32_t tid = threadIdx.x, B = blockDim.x;
     __threadfence();
     __syncthreads();
     __shared__ unsigned int is_last;
@@ -97,7 +109,6 @@ __device__ __forceinline__ void reduce_group(const uint32_t (&acc)[C][4], const 
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    const uint32_t lanes = 4 * tpr, base = blockIdx.y * lanes;
     for (uint32_t li = tid; li < lanes; li += B) fin(base + li);
     if (tid == 0) red.ticket[blockIdx.y] = 0u;
     if (red.done) {
@@ -105,6 +116,26 @@ __device__ __forceinline__ void reduce_group(const uint32_t (&acc)[C][4], const 
         __syncthreads();
         if (tid == 0) atomicAdd_system(red.done, 1u);
     }
+}
+
+// reduce_group for kernels with one copy per thread: g.tpr threads (copies) per row slice,
+// acc[c] the thread's canonical partial of component c for copy blockIdx.y * g.tpr + q.
+template <int C, class Fin>
+__device__ __forceinline__ void reduce_group1(const uint32_t (&acc)[C], const Geo& g, bool active, RedScratch red,
+                                              Fin fin) {
+    extern __shared__ uint32_t smem[];
+    const uint32_t tid = threadIdx.x, B = blockDim.x, L = g.tpr, rps = g.rps;
+#pragma unroll
+    for (int c = 0; c < C; c++) smem[c * B + tid] = active ? acc[c] : 0u;
+    __syncthreads();
+    for (uint32_t o = tid; o < (uint32_t)C * L; o += B) {
+        const uint32_t c = o / L, q = o - c * L;
+        const uint32_t* col = smem + c * B + q;
+        unsigned long long s = 0;
+        for (uint32_t r = 0; r < rps; r++) s += col[r * L];
+        atomicAdd(&red.acc[(size_t)c * g.N + blockIdx.y * L + q], s);
+    }
+    finish_group(red, blockIdx.y * L, L, fin);
 }
 
 struct TileIdx {
@@ -797,6 +828,11 @@ __device__ __forceinline__ uint64_t fold64(uint64_t x) {
     return ((uint64_t)nh << 32) | nl;
 }
 
+// acc += a * b with one 32 x 32 -> 64-bit multiply-add.
+__device__ __forceinline__ void mad64(uint64_t& acc, uint32_t a, uint32_t b) {
+    asm("mad.wide.u32 %0, %1, %2, %0;" : "+l"(acc) : "r"(a), "r"(b));
+}
+
 // Phase-two round 0 (no fold): p0_j = sum f(2i) s_j(2i), p1_j = sum f(2i+1) s_j(2i+1),
 // p2raw_j = sum (f(2i) + f(2i+1)) (s_j(2i) + s_j(2i+1)) over the layer input f = v, for
 // all R repetitions in one thread so that each row read serves the R scalar tables.  With
@@ -890,6 +926,207 @@ __global__ void __launch_bounds__(256, 2) k_p2_round0(P2Src src, uint64_t npairs
     reduce_group<3 * R>(out, g, t.active, red, 0, RoundFin{red, evals_out, vx, g.N, (uint32_t)R});
 }
 
+// ---------------------------------------------------------------- phase two: rounds 0 and 1 in one pass
+// Round 1 folds the layer input v and the scalar tables s_j at the round-0 challenge r
+// (receive_challenge, sumcheck_helper.hpp:104-133), so its sums are quadratic in r.  Over a
+// group of four input rows y = 4i..4i+3 (values v0..v3, scalars s0..s3), round 1's pair is
+// f0 = (1-r) v0 + r v1, f1 = (1-r) v2 + r v3 (h0, h1 alike from s), and
+//   p0_1    = sum f0 h0             = (1-r)^2 E00 + r(1-r) KE + r^2 E11,
+//   p1_1    = sum f1 h1             = (1-r)^2 F22 + r(1-r) KF + r^2 F33,
+//   p2raw_1 = sum (f0 + f1)(h0 + h1) = (1-r)^2 U00 + r(1-r) KU + r^2 U11,
+// with E00 = sum v0 s0, E11 = sum v1 s1, KE = sum v0 s1 + v1 s0 (F.. from rows 2, 3), and
+// U.. the same over u0 = v0 + v2, u1 = v1 + v3 and t0 = s0 + s2, t1 = s1 + s3.  Round 0's
+// sums (poly_eval_at over the pairs (4i, 4i+1), (4i+2, 4i+3), sumcheck_helper.hpp:68-102)
+// are p0_0 = E00 + F22, p1_0 = E11 + F33, p2raw_0 = E00 + E11 + KE + F22 + F33 + KF.
+// One pass over v therefore yields both rounds: the finisher writes round 0's evaluations
+// (times v(rx), since h = v(rx) s) for the transcript and the 9R canonical sums to `sums`,
+// and k_p2_round1_fin evaluates round 1 from them once r is known — round 1 never reads v.
+// One copy per thread (9R unreduced 64-bit sums: every sum is folded by fold64 before it can
+// hold more than four products).  A warp covers 32 consecutive copies of one row group and
+// stages it kP01Stages - 1 groups ahead with one 16-byte cp.async per thread (row wl / 8,
+// copies 4 (wl % 8) ..), plus the group's scalars (s0..s3) and (t0, t1, 0, 0) of each
+// repetition from lanes 0 .. 2R-1; after the wait a __syncwarp makes the whole slot
+// visible and each thread reads its copy's four values transposed.
+constexpr int kP01Stages = 8;
+constexpr int kP01Sums = 9;       // E00, E11, KE, F22, F33, KF, U00, U11, KU
+constexpr int kP01WarpSlot = 608;  // bytes per warp and stage: 4 rows x 32 copies x 4 B + 6 x 16 B scalars
+
+struct P01Src {
+    const uint32_t* v;     // the layer input, 4 ngroups rows
+    const uint32_t* s[3];  // s_j: 4 ngroups scalars (s0..s3 of each group)
+    const uint32_t* t[3];  // (t0, t1, 0, 0) of each group: 4 ngroups scalars
+};
+
+// Round 0's evaluations from the nine sums of each repetition, times v(rx); the sums are
+// kept canonical in `sums` for round 1.
+struct P01Fin {
+    RedScratch red;
+    uint32_t* out;       // R x 3 x N
+    const uint32_t* vx;  // R x N
+    uint32_t* sums;      // 9R x N
+    uint32_t N, reps;
+    __device__ void operator()(uint32_t lane) const {
+        for (uint32_t j = 0; j < reps; j++) {
+            uint32_t m[kP01Sums];
+#pragma unroll
+            for (int k = 0; k < kP01Sums; k++) {
+                m[k] = take(red, kP01Sums * j + k, N, lane);
+                sums[(size_t)(kP01Sums * j + k) * N + lane] = m[k];
+            }
+            const uint32_t p0 = add(m[0], m[3]), p1 = add(m[1], m[4]);
+            const uint32_t p2raw = add(add(p0, p1), add(m[2], m[5]));
+            const uint32_t x = vx[(size_t)j * N + lane];
+            out[(size_t)(3 * j) * N + lane] = mul(p0, x);
+            out[(size_t)(3 * j + 1) * N + lane] = mul(p1, x);
+            out[(size_t)(3 * j + 2) * N + lane] = mul(m31::eval_at_two(p0, p1, p2raw), x);
+        }
+    }
+};
+
+template <int R>
+__global__ void __launch_bounds__(256, 2) k_p2_round01(P01Src src, uint64_t ngroups, const uint32_t* __restrict__ vx,
+                                                       Geo g, RedScratch red, uint32_t* evals_out, uint32_t* sums_out) {
+    extern __shared__ uint4 ring01[];  // kP01Stages x warps x kP01WarpSlot bytes
+    const uint32_t tid = threadIdx.x, wl = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+    const uint32_t L = g.tpr, rs = tid / L;  // L: copies per row slice, a multiple of 32
+    const bool active = rs < g.rps;          // uniform over a warp
+    const uint64_t N = g.N;
+    // this thread's global copy, and the 16 bytes it stages: row wl / 8 of the group, copies
+    // 4 (wl % 8) .. of the warp's 32
+    const uint64_t warp_lane0 = (uint64_t)blockIdx.y * L + (tid - rs * L - wl);
+    const uint32_t* __restrict__ vst = src.v + (wl >> 3) * N + warp_lane0 + 4 * (wl & 7);
+    const uint32_t* __restrict__ sst = nullptr;
+    if (wl < 2 * R) {
+        const uint32_t j = wl >> 1;
+        sst = (wl & 1) ? (j == 0 ? src.t[0] : (j == 1 ? src.t[1] : src.t[2]))
+                       : (j == 0 ? src.s[0] : (j == 1 ? src.s[1] : src.s[2]));
+    }
+    char* const ring = reinterpret_cast<char*>(ring01);
+    uint64_t acc[R * kP01Sums];
+#pragma unroll
+    for (int c = 0; c < R * kP01Sums; c++) acc[c] = 0ull;
+    if (active) {
+        const uint64_t step = (uint64_t)gridDim.x * g.rps;
+        const uint64_t i0 = (uint64_t)blockIdx.x * g.rps + rs;
+        auto stage = [&](uint64_t i, int slot) {
+            if (i < ngroups) {
+                char* st = ring + ((size_t)slot * nw + w) * kP01WarpSlot;
+                cp_async16(st + 16 * wl, vst + 4 * i * N);
+                if (sst) cp_async16(st + 512 + 16 * wl, sst + 4 * i);
+            }
+            cp_async_commit();  // one group per iteration, empty past the end
+        };
+#pragma unroll
+        for (int s = 0; s < kP01Stages - 1; s++) stage(i0 + s * step, s);
+        int slot = 0;
+        uint32_t it = 0;
+        for (uint64_t i = i0; i < ngroups; i += step, it++) {
+            __syncwarp();  // every lane has read the slot refilled next
+            stage(i + (kP01Stages - 1) * step, slot == 0 ? kP01Stages - 1 : slot - 1);
+            cp_async_wait<kP01Stages - 1>();
+            __syncwarp();  // the other lanes' copies of this slot are visible
+            const char* st = ring + ((size_t)slot * nw + w) * kP01WarpSlot;
+            const uint32_t* rows = reinterpret_cast<const uint32_t*>(st);
+            const uint32_t x0 = rows[wl], x1 = rows[32 + wl], x2 = rows[64 + wl], x3 = rows[96 + wl];
+            const uint4* sc = reinterpret_cast<const uint4*>(st + 512);
+            const uint32_t u0 = add(x0, x2), u1 = add(x1, x3);
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                const uint4 sv = sc[2 * j], tv = sc[2 * j + 1];
+                uint64_t* a = acc + kP01Sums * j;
+                mad64(a[0], x0, sv.x);
+                mad64(a[1], x1, sv.y);
+                mad64(a[2], x0, sv.y);
+                mad64(a[2], x1, sv.x);
+                mad64(a[3], x2, sv.z);
+                mad64(a[4], x3, sv.w);
+                mad64(a[5], x2, sv.w);
+                mad64(a[5], x3, sv.z);
+                mad64(a[6], u0, tv.x);
+                mad64(a[7], u1, tv.y);
+                mad64(a[8], u0, tv.y);
+                mad64(a[8], u1, tv.x);
+            }
+            // a K sum gains two products per group, the others one: folding the K sums every
+            // second group and the others every fourth keeps each below 2^34 + 4 (p - 1)^2 < 2^64
+            if (it & 1) {
+#pragma unroll
+                for (int j = 0; j < R; j++) {
+                    acc[kP01Sums * j + 2] = fold64(acc[kP01Sums * j + 2]);
+                    acc[kP01Sums * j + 5] = fold64(acc[kP01Sums * j + 5]);
+                    acc[kP01Sums * j + 8] = fold64(acc[kP01Sums * j + 8]);
+                }
+            }
+            if ((it & 3) == 3) {
+#pragma unroll
+                for (int j = 0; j < R; j++) {
+#pragma unroll
+                    for (int k = 0; k < kP01Sums; k++)
+                        if (k % 3 != 2) acc[kP01Sums * j + k] = fold64(acc[kP01Sums * j + k]);
+                }
+            }
+            slot = slot + 1 == kP01Stages ? 0 : slot + 1;
+        }
+        cp_async_wait<0>();
+    }
+    uint32_t out[R * kP01Sums];
+#pragma unroll
+    for (int c = 0; c < R * kP01Sums; c++) out[c] = reduce64(acc[c]);
+    __syncthreads();  // the ring is reused as the reduction's scratch
+    reduce_group1<R * kP01Sums>(out, g, active, red, P01Fin{red, evals_out, vx, sums_out, g.N, (uint32_t)R});
+}
+
+// Round 1 of phase two at the round-0 challenges r_j from the sums of k_p2_round01: block 0
+// evaluates every copy's p0_1, p1_1, p2_1 (times v(rx)) and publishes them like a round
+// kernel's finisher; the other blocks fold the scalar tables at r_j for round 2,
+// s'_j(2i) = fold(s_j(4i), s_j(4i+1), r_j), s'_j(2i+1) = fold(s_j(4i+2), s_j(4i+3), r_j).
+struct P1Fold {
+    const uint32_t* s[3];
+    uint32_t* sd[3];
+    uint32_t r[3];
+};
+
+__global__ void __launch_bounds__(256) k_p2_round1_fin(const uint32_t* __restrict__ sums, const uint32_t* __restrict__ vx,
+                                                       P1Fold f, uint64_t ngroups, uint32_t N, uint32_t reps,
+                                                       uint32_t* evals_out, unsigned int* done) {
+    const uint32_t tid = threadIdx.x, B = blockDim.x;
+    if (blockIdx.x == 0) {
+        for (uint32_t j = 0; j < reps; j++) {
+            const uint32_t r = j == 0 ? f.r[0] : (j == 1 ? f.r[1] : f.r[2]);
+            const uint32_t omr = sub(1u, r);
+            const uint32_t c0 = mul(omr, omr), c1 = mul(r, omr), c2 = mul(r, r);
+            for (uint32_t lane = tid; lane < N; lane += B) {
+                uint32_t m[kP01Sums];
+#pragma unroll
+                for (int k = 0; k < kP01Sums; k++) m[k] = __ldg(sums + (size_t)(kP01Sums * j + k) * N + lane);
+                const uint32_t p0 = add(add(mul(c0, m[0]), mul(c1, m[2])), mul(c2, m[1]));
+                const uint32_t p1 = add(add(mul(c0, m[3]), mul(c1, m[5])), mul(c2, m[4]));
+                const uint32_t p2raw = add(add(mul(c0, m[6]), mul(c1, m[8])), mul(c2, m[7]));
+                const uint32_t x = __ldg(vx + (size_t)j * N + lane);
+                evals_out[(size_t)(3 * j) * N + lane] = mul(p0, x);
+                evals_out[(size_t)(3 * j + 1) * N + lane] = mul(p1, x);
+                evals_out[(size_t)(3 * j + 2) * N + lane] = mul(m31::eval_at_two(p0, p1, p2raw), x);
+            }
+        }
+        if (done) {
+            __threadfence_system();
+            __syncthreads();
+            if (tid == 0) atomicAdd_system(done, 1u);
+        }
+        return;
+    }
+    const uint64_t total = (uint64_t)reps * ngroups, stride = (uint64_t)(gridDim.x - 1) * B;
+    for (uint64_t idx = (uint64_t)(blockIdx.x - 1) * B + tid; idx < total; idx += stride) {
+        const uint32_t j = (uint32_t)(idx / ngroups);
+        const uint64_t i = idx - (uint64_t)j * ngroups;
+        const uint32_t r = j == 0 ? f.r[0] : (j == 1 ? f.r[1] : f.r[2]);
+        const uint32_t* sj = j == 0 ? f.s[0] : (j == 1 ? f.s[1] : f.s[2]);
+        uint32_t* dj = j == 0 ? f.sd[0] : (j == 1 ? f.sd[1] : f.sd[2]);
+        const uint4 sv = __ldg(reinterpret_cast<const uint4*>(sj) + i);
+        reinterpret_cast<uint2*>(dj)[i] = make_uint2(fold(sv.x, sv.y, r), fold(sv.z, sv.w, r));
+    }
+}
+
 // ---------------------------------------------------------------- phase two: s(y)
 // s_j[y] = sum over mul gates (z, x, y, c) of eqc_j[z] * eq_rx_j[x] * c: the
 // copy-independent factor of h(y) = v(rx) s(y) (sumcheck_helper.hpp:250-259).
@@ -908,6 +1145,35 @@ __global__ void k_s_build(uint64_t I, uint64_t O, const uint32_t* __restrict__ m
             }
         }
         for (uint32_t j = 0; j < reps; j++) s_out[(uint64_t)j * s_stride + y] = s[j];
+    }
+}
+
+// k_s_build over groups of four rows (I a multiple of 4), one thread per group, which also
+// writes t_j(i) = (s_j(4i) + s_j(4i+2), s_j(4i+1) + s_j(4i+3), 0, 0), the scalar pair sums
+// that k_p2_round01 stages with each group.
+__global__ void k_s_build4(uint64_t I, uint64_t O, const uint32_t* __restrict__ my_off, const uint4* __restrict__ my_g,
+                           const uint32_t* __restrict__ eqc, const uint32_t* __restrict__ eqrx, uint32_t* __restrict__ s_out,
+                           uint32_t* __restrict__ t_out, uint64_t s_stride, uint32_t reps) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x, ngroups = I / 4;
+    for (uint64_t gi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gi < ngroups; gi += stride) {
+        uint32_t s[3][4] = {};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint64_t y = 4 * gi + k;
+            const uint32_t k0 = __ldg(my_off + y), k1 = __ldg(my_off + y + 1);
+            for (uint32_t e = k0; e < k1; e++) {
+                const uint4 gt = __ldg(my_g + e);  // (x, z, c, 0)
+                for (uint32_t j = 0; j < reps; j++) {
+                    const uint32_t w = mul(__ldg(eqc + (uint64_t)j * O + gt.y), __ldg(eqrx + (uint64_t)j * I + gt.x));
+                    s[j][k] = add(s[j][k], mul(w, gt.z));
+                }
+            }
+        }
+        for (uint32_t j = 0; j < reps; j++) {
+            reinterpret_cast<uint4*>(s_out + (uint64_t)j * s_stride)[gi] = make_uint4(s[j][0], s[j][1], s[j][2], s[j][3]);
+            reinterpret_cast<uint4*>(t_out + (uint64_t)j * s_stride)[gi] =
+                make_uint4(add(s[j][0], s[j][2]), add(s[j][1], s[j][3]), 0u, 0u);
+        }
     }
 }
 
@@ -1149,6 +1415,71 @@ cudaError_t launch_p2_round2(int reps, const RoundPtrs& p, uint64_t npairs, cons
         case 3: k_p2_round2<3><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out); break;
         default: return cudaErrorInvalidValue;
     }
+    return cudaGetLastError();
+}
+
+// Lanes per row slice of the one-copy-per-thread kernels: the largest divisor of N up to 256.
+static uint32_t one_copy_slice(uint32_t N) {
+    uint32_t L = N < 256 ? N : 256;
+    while (L > 1 && N % L) L--;
+    return L;
+}
+
+uint32_t p2_round01_groups(uint32_t N) {
+    const uint32_t L = N ? one_copy_slice(N) : 1;
+    return L % 32 ? 0 : N / L;
+}
+
+cudaError_t launch_p2_round01(int reps, const uint32_t* v, const uint32_t* const* s, const uint32_t* const* t,
+                              uint64_t ngroups, const uint32_t* vx, uint32_t N, uint32_t ctas, RedScratch red,
+                              uint32_t* evals_out, uint32_t* sums_out, cudaStream_t st) {
+    if (reps < 1 || reps > 3 || p2_round01_groups(N) == 0) return cudaErrorInvalidValue;
+    if ((reinterpret_cast<uintptr_t>(v) & 15) != 0) return cudaErrorInvalidValue;  // 16-byte cp.async
+    Geo g;
+    g.N = N;
+    g.tpr = one_copy_slice(N);
+    g.rps = 256 / g.tpr;
+    const uint32_t groups = N / g.tpr;
+    uint64_t need = (ngroups + g.rps - 1) / g.rps, cap = ctas / groups;
+    if (cap < 1) cap = 1;
+    if (need < 1) need = 1;
+    const dim3 grid((uint32_t)(need < cap ? need : cap), groups, 1);
+    const size_t ring = (size_t)kP01Stages * 8 * kP01WarpSlot, red_b = (size_t)3 * kP01Sums * 4 * 256;
+    const size_t smem = ring > red_b ? ring : red_b;
+    P01Src src;
+    src.v = v;
+    for (int j = 0; j < 3; j++) {
+        src.s[j] = j < reps ? s[j] : nullptr;
+        src.t[j] = j < reps ? t[j] : nullptr;
+    }
+    switch (reps) {
+        case 1: k_p2_round01<1><<<grid, 256, smem, st>>>(src, ngroups, vx, g, red, evals_out, sums_out); break;
+        case 2: k_p2_round01<2><<<grid, 256, smem, st>>>(src, ngroups, vx, g, red, evals_out, sums_out); break;
+        default: k_p2_round01<3><<<grid, 256, smem, st>>>(src, ngroups, vx, g, red, evals_out, sums_out); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_p2_round1_fin(int reps, const uint32_t* sums, const uint32_t* vx, const uint32_t* const* s,
+                                 uint32_t* const* sd, const uint32_t* r, uint64_t ngroups, uint32_t N,
+                                 uint32_t* evals_out, unsigned int* done, cudaStream_t st) {
+    if (reps < 1 || reps > 3) return cudaErrorInvalidValue;
+    P1Fold f;
+    for (int j = 0; j < 3; j++) {
+        f.s[j] = j < reps ? s[j] : nullptr;
+        f.sd[j] = j < reps ? sd[j] : nullptr;
+        f.r[j] = j < reps ? r[j] : 0u;
+    }
+    const uint32_t fold_blocks = grid_1d((uint64_t)reps * ngroups, 256);
+    k_p2_round1_fin<<<1 + fold_blocks, 256, 0, st>>>(sums, vx, f, ngroups, N, (uint32_t)reps, evals_out, done);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_s_build4(uint64_t I, uint64_t O, const uint32_t* my_off, const uint4* my_g, const uint32_t* eqc,
+                            const uint32_t* eqrx, uint32_t* s_out, uint32_t* t_out, uint64_t s_stride, uint32_t reps,
+                            cudaStream_t s) {
+    if (I % 4 || (s_stride % 4)) return cudaErrorInvalidValue;
+    k_s_build4<<<grid_1d(I / 4, 256), 256, 0, s>>>(I, O, my_off, my_g, eqc, eqrx, s_out, t_out, s_stride, reps);
     return cudaGetLastError();
 }
 

@@ -125,6 +125,28 @@ cudaError_t launch_p2_round2(int reps, const RoundPtrs& p, uint64_t npairs, cons
 cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold, const RoundPtrs& p, uint64_t npairs,
                          const uint32_t* vx, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
                          uint32_t* evals_out, cudaStream_t s);
+// Phase-two rounds 0 and 1 in one pass over the layer input v (4 ngroups rows, ngroups >= 2):
+// round 0's evaluations (times vx) are published to evals_out as by the round kernels, and
+// 9 * reps canonical sums per copy go to sums_out (9 reps x N) for launch_p2_round1_fin.
+// s[j] are the scalar tables (16-byte aligned), t[j] their pair sums (launch_s_build4);
+// red.acc needs 9 * reps x N accumulators.  Publishes p2_round01_groups(N) lane groups;
+// p2_round01_groups(N) is 0 where the kernel does not apply (its row slices of up to 256
+// copies must be a multiple of 32 copies).
+cudaError_t launch_p2_round01(int reps, const uint32_t* v, const uint32_t* const* s, const uint32_t* const* t,
+                              uint64_t ngroups, const uint32_t* vx, uint32_t N, uint32_t ctas, RedScratch red,
+                              uint32_t* evals_out, uint32_t* sums_out, cudaStream_t st);
+uint32_t p2_round01_groups(uint32_t N);
+// Phase-two round 1 from those sums at the round-0 challenges r[j]: evaluations to evals_out
+// (one completion count on done), and the scalar tables s[j] folded into sd[j] (2 ngroups
+// entries each) for round 2.
+cudaError_t launch_p2_round1_fin(int reps, const uint32_t* sums, const uint32_t* vx, const uint32_t* const* s,
+                                 uint32_t* const* sd, const uint32_t* r, uint64_t ngroups, uint32_t N,
+                                 uint32_t* evals_out, unsigned int* done, cudaStream_t st);
+// launch_s_build plus the pair sums t_j(i) = (s_j(4i) + s_j(4i+2), s_j(4i+1) + s_j(4i+3), 0, 0)
+// into t_out (4 I/4 entries, stride s_stride); I and s_stride multiples of 4.
+cudaError_t launch_s_build4(uint64_t I, uint64_t O, const uint32_t* my_off, const uint4* my_g, const uint32_t* eqc,
+                            const uint32_t* eqrx, uint32_t* s_out, uint32_t* t_out, uint64_t s_stride, uint32_t reps,
+                            cudaStream_t s);
 cudaError_t launch_s_build(uint64_t I, uint64_t O, const uint32_t* my_off, const uint4* my_g, const uint32_t* eqc,
                            const uint32_t* eqrx, uint32_t* s_out, uint64_t s_stride, uint32_t reps, cudaStream_t s);
 cudaError_t launch_wsum(int reps, const uint32_t* vals, uint64_t rows, const uint32_t* eq, const Geo& g,

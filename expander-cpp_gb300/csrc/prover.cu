@@ -27,6 +27,7 @@
 #include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <memory>
@@ -227,7 +228,11 @@ struct Lane {
     struct Rec {
         int kid;
         size_t e0, e1;
+        double bytes;
+        uint32_t tag;
     };
+    // (layer << 16) | (phase << 8) | round of the launches that follow, for the trace
+    uint32_t tag = 0;
     std::vector<cudaEvent_t> events;
     size_t ev_used = 0;
     std::vector<Rec> recs;
@@ -385,10 +390,14 @@ struct gkrgpu_ctx {
     uint64_t launches[K_NUM_KERNELS] = {};
     double ms[K_NUM_KERNELS] = {};
     double bytes[K_NUM_KERNELS] = {};
+    // per-launch CSV (kernel, layer, phase, round, algorithmic bytes, ms) of timed jobs,
+    // appended to the file named by the environment variable GKRGPU_TRACE
+    FILE* trace = nullptr;
 
     ~gkrgpu_ctx() {
         DeviceGuard g(device);
         lanes.clear();
+        if (trace) fclose(trace);
         for (auto e : markers)
             if (e) cudaEventDestroy(e);
         if (pool) cudaMemPoolDestroy(pool);
@@ -443,7 +452,7 @@ void Lane::launch(int kid, double algo_bytes, F&& f) {
     if (X->timing) {
         const size_t e1 = next_event();
         ck(cudaEventRecord(events[e1], stream), "cudaEventRecord");
-        recs.push_back({kid, e0, e1});
+        recs.push_back({kid, e0, e1, algo_bytes, tag});
     }
 }
 
@@ -451,14 +460,20 @@ void Lane::launch(int kid, double algo_bytes, F&& f) {
 // the stream must be idle.
 void Lane::resolve_events() {
     double t_ms[K_NUM_KERNELS] = {};
-    for (const Rec& r : recs) {
-        float t = 0.f;
-        ck(cudaEventElapsedTime(&t, events[r.e0], events[r.e1]), "cudaEventElapsedTime");
-        t_ms[r.kid] += t;
+    std::vector<float> each(recs.size());
+    for (size_t i = 0; i < recs.size(); i++) {
+        const Rec& r = recs[i];
+        ck(cudaEventElapsedTime(&each[i], events[r.e0], events[r.e1]), "cudaEventElapsedTime");
+        t_ms[r.kid] += each[i];
     }
+    std::lock_guard<std::mutex> lk(X->stats_m);
+    if (X->trace)
+        for (size_t i = 0; i < recs.size(); i++)
+            fprintf(X->trace, "%s,%u,%u,%u,%.0f,%.6f\n", kKernelNames[recs[i].kid], recs[i].tag >> 16,
+                    (recs[i].tag >> 8) & 0xff, recs[i].tag & 0xff, recs[i].bytes, (double)each[i]);
+    if (X->trace) fflush(X->trace);
     recs.clear();
     ev_used = 0;
-    std::lock_guard<std::mutex> lk(X->stats_m);
     for (int k = 0; k < K_NUM_KERNELS; k++) {
         X->launches[k] += job_launches[k];
         X->bytes[k] += job_bytes[k];
@@ -632,6 +647,7 @@ struct Workspace {
     uint32_t *hg0[3] = {}, *hgA[3] = {}, *fA[3] = {}, *fB[3] = {};
     uint32_t* sb[2] = {};
     uint32_t *eqc = nullptr, *eqrx = nullptr, *evals = nullptr, *vx = nullptr, *cv = nullptr;
+    uint32_t* p2s = nullptr;  // 9R x N sums of phase-two rounds 0 and 1 (launch_p2_round01)
     uint4 *a4 = nullptr, *w4 = nullptr;
     unsigned long long* acc = nullptr;
     unsigned int* ticket = nullptr;
@@ -665,13 +681,14 @@ struct Workspace {
             eqrx = (uint32_t*)take(R * maxI * 4);
             a4 = (uint4*)take(maxI * 16);
             w4 = (uint4*)take(std::max<uint64_t>(C.max_mul, 1) * 16);
+            p2s = (uint32_t*)take(27ull * N * 4);
         }
         eqc = (uint32_t*)take(R * maxO * 4);
         evals = (uint32_t*)take(9ull * N * 4);
         vx = (uint32_t*)take(3ull * N * 4);
         cv = (uint32_t*)take(3ull * N * 4);
         zero_off = o;
-        acc = (unsigned long long*)take(9ull * N * 8);
+        acc = (unsigned long long*)take(27ull * N * 8);  // up to 9R components (launch_p2_round01)
         ticket = (unsigned int*)take(4096);
         flag = (unsigned int*)take(16);
         zero_bytes = o - zero_off;
@@ -758,6 +775,7 @@ struct Prover {
             const DevLayer& Ly = C.layers[l];
             const uint64_t O = 1ull << Ly.nout;
             const double b = 4.0 * N * (2.0 * Ly.nmul + Ly.nadd + O) + 16.0 * Ly.nmul + 8.0 * Ly.nadd + 8.0 * (O + 1);
+            c.tag = (uint32_t)l << 16;
             c.launch(K_EVALUATE, b, [&] {
                 return launch_evaluate(vals[l], vals[l + 1], O, Ly.mo_off, Ly.mo_g, Ly.ao_off, Ly.ao_g,
                                        gk[K_EVALUATE], X.block, ck_ctas[K_EVALUATE], c.stream);
@@ -834,6 +852,7 @@ struct Prover {
         std::vector<uint32_t> vy((size_t)R * N);
 
         // phase one: eqc_j = alpha eq(rz1_j) + beta eq(rz2_j), gate weights, hg + round 0
+        c.tag = ((uint32_t)li << 16) | (1u << 8);
         eq_table(ws.eqc, rz1, rz2, alpha, beta, m);
         const double wb = 32.0 * Ly.nmul + 20.0 * I + 8.0 * Ly.nadd + 4.0 * R * (Ly.nmul + Ly.nadd);
         c.launch(K_WEIGHTS, wb, [&] {
@@ -864,6 +883,7 @@ struct Prover {
             }
             const uint64_t npairs = I >> (k + 1);
             const double S = 4.0 * npairs;
+            c.tag = ((uint32_t)li << 16) | (1u << 8) | k;
             int kid = K_ROUND_LANE;
             if (k == 1) {
                 // hg rebuilt from the weights: v read once, the gathers again, f and hg halves out
@@ -906,13 +926,44 @@ struct Prover {
         }
 
         // phase two: h(y) = vx * s(y)
+        c.tag = ((uint32_t)li << 16) | (2u << 8);
         eq_table(ws.eqrx, rx, nullptr, 1u, 0u, n);
         const size_t sstride = ws.sstride;
-        c.launch(K_S_BUILD, 16.0 * Ly.nmul + 4.0 * I + 4.0 * R * I + 8.0 * R * Ly.nmul, [&] {
-            return launch_s_build(I, O, Ly.my_off, Ly.my_g, ws.eqc, ws.eqrx, ws.sb[0], sstride, R, c.stream);
-        });
+        // with at least three rounds, rounds 0 and 1 come from one pass over the layer input
+        // (their sums are quadratic in round 0's challenge) and round 2 refolds the input
+        const bool fused01 = n >= 3 && p2_round01_groups(N) > 0;
+        const bool refold = n >= 3;
+        c.launch(K_S_BUILD, 16.0 * Ly.nmul + 4.0 * I + 4.0 * R * I + 8.0 * R * Ly.nmul + (fused01 ? 4.0 * R * I : 0.0),
+                 [&] {
+                     return fused01 ? launch_s_build4(I, O, Ly.my_off, Ly.my_g, ws.eqc, ws.eqrx, ws.sb[0], ws.sb[1],
+                                                      sstride, R, c.stream)
+                                    : launch_s_build(I, O, Ly.my_off, Ly.my_g, ws.eqc, ws.eqrx, ws.sb[0], sstride,
+                                                     R, c.stream);
+                 });
         c.copy(ws.vx, vxh, R * rowb, cudaMemcpyHostToDevice, "vx upload");
-        {
+        uint32_t k_first = 1;
+        if (fused01) {
+            const uint64_t ngroups = I / 4;
+            const uint32_t* sj[3] = {ws.sb[0], ws.sb[0] + sstride, ws.sb[0] + 2 * sstride};
+            const uint32_t* tj[3] = {ws.sb[1], ws.sb[1] + sstride, ws.sb[1] + 2 * sstride};
+            c.launch(K_P2_ROUND0, rb * I + 8.0 * R * I + 4.0 * 9 * R * N, [&] {
+                return launch_p2_round01(R, v, sj, tj, ngroups, ws.vx, N, ck_ctas[K_P2_ROUND0], red_mapped(),
+                                         c.evals_d(), ws.p2s, c.stream);
+            });
+            fetch(p2_round01_groups(N), nullptr, true);
+            transcript_round(t, ry, 0, false, false, vy.data());
+            // round 1 from the sums; the scalar tables folded at ry_j[0] replace the pair sums
+            c.tag = ((uint32_t)li << 16) | (2u << 8) | 1u;
+            uint32_t* sd[3] = {ws.sb[1], ws.sb[1] + sstride, ws.sb[1] + 2 * sstride};
+            uint32_t r0[3] = {ry[0][0], R > 1 ? ry[1][0] : 0u, R > 2 ? ry[2][0] : 0u};
+            c.launch(K_ROUND_SCALAR, 4.0 * 9 * R * N + 4.0 * R * N + 6.0 * R * I, [&] {
+                return launch_p2_round1_fin(R, ws.p2s, ws.vx, sj, sd, r0, ngroups, N, c.evals_d(), c.done_d(),
+                                            c.stream);
+            });
+            fetch(1, nullptr, false);
+            transcript_round(t, ry, 1, false, false, vy.data());
+            k_first = 2;
+        } else {
             RoundPtrs p;
             memset(&p, 0, sizeof(p));
             p.fsrc[0] = v;
@@ -926,7 +977,7 @@ struct Prover {
             transcript_round(t, ry, 0, n == 1, false, vy.data());
         }
         for (int j = 0; j < R; j++) cur_f[j] = v;
-        for (uint32_t k = 1; k < n; k++) {
+        for (uint32_t k = k_first; k < n; k++) {
             RoundPtrs p;
             memset(&p, 0, sizeof(p));
             const int src = (k - 1) & 1, dst = k & 1;
@@ -939,9 +990,9 @@ struct Prover {
             }
             const uint64_t npairs = I >> (k + 1);
             const double S = 4.0 * npairs;
-            // with a round 2, round 1 stores only its scalar tables and round 2 refolds the
-            // layer input (the round-1 copies would be written once and read once)
-            const bool refold = n >= 3;
+            c.tag = ((uint32_t)li << 16) | (2u << 8) | k;
+            // with a round 2, round 1 stores no folded copies (they would be written once and
+            // read once): round 2 refolds the layer input
             if (k == 1 && refold)
                 for (int j = 0; j < R; j++) p.fdst[j] = nullptr;
             if (k == 2 && refold) {
@@ -1353,6 +1404,8 @@ int gkrgpu_create(int device, gkrgpu_ctx** out) {
         ck(cudaMemPoolCreate(&c->pool, &pp), "cudaMemPoolCreate");
         uint64_t keep = c->hbm_budget;
         ck(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
+        if (const char* tp = getenv("GKRGPU_TRACE"))
+            if (*tp) c->trace = fopen(tp, "a");
         c->lane(0);
         *out = c.release();
     });
