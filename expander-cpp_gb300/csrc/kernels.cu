@@ -808,10 +808,21 @@ __global__ void __launch_bounds__(256) k_p2_round2(RoundPtrs p, uint64_t npairs,
                 }
                 st4(p.fdst[j], 2 * i, g.N, t.lane0, mk4(f0));
                 st4(p.fdst[j], 2 * i + 1, g.N, t.lane0, mk4(f1));
-                accum_pair(*reinterpret_cast<uint32_t(*)[3][4]>(&acc[3 * j]), f0, f1, h0, h1);
+                // sums kept below 2^32 without reduction (mac_lazy), canonical at the end
+                const uint32_t hs = add(s0, s1);
+#pragma unroll
+                for (int l = 0; l < 4; l++) {
+                    acc[3 * j][l] = m31::mac_lazy(acc[3 * j][l], f0[l], h0[l]);
+                    acc[3 * j + 1][l] = m31::mac_lazy(acc[3 * j + 1][l], f1[l], h1[l]);
+                    acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], add(f0[l], f1[l]), hs);
+                }
             }
         }
     }
+#pragma unroll
+    for (int c = 0; c < 3 * R; c++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[c][l] = m31::from_u32(acc[c][l]);
     reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, vx, g.N, (uint32_t)R});
 }
 
@@ -934,27 +945,29 @@ __global__ void __launch_bounds__(256, 2) k_p2_round0(P2Src src, uint64_t npairs
 //   p0_1    = sum f0 h0             = (1-r)^2 E00 + r(1-r) KE + r^2 E11,
 //   p1_1    = sum f1 h1             = (1-r)^2 F22 + r(1-r) KF + r^2 F33,
 //   p2raw_1 = sum (f0 + f1)(h0 + h1) = (1-r)^2 U00 + r(1-r) KU + r^2 U11,
-// with E00 = sum v0 s0, E11 = sum v1 s1, KE = sum v0 s1 + v1 s0 (F.. from rows 2, 3), and
-// U.. the same over u0 = v0 + v2, u1 = v1 + v3 and t0 = s0 + s2, t1 = s1 + s3.  Round 0's
-// sums (poly_eval_at over the pairs (4i, 4i+1), (4i+2, 4i+3), sumcheck_helper.hpp:68-102)
-// are p0_0 = E00 + F22, p1_0 = E11 + F33, p2raw_0 = E00 + E11 + KE + F22 + F33 + KF.
-// One pass over v therefore yields both rounds: the finisher writes round 0's evaluations
-// (times v(rx), since h = v(rx) s) for the transcript and the 9R canonical sums to `sums`,
-// and k_p2_round1_fin evaluates round 1 from them once r is known — round 1 never reads v.
-// One copy per thread (9R unreduced 64-bit sums: every sum is folded by fold64 before it can
-// hold more than four products).  A warp covers 32 consecutive copies of one row group and
-// stages it kP01Stages - 1 groups ahead with one 16-byte cp.async per thread (row wl / 8,
-// copies 4 (wl % 8) ..), plus the group's scalars (s0..s3) and (t0, t1, 0, 0) of each
-// repetition from lanes 0 .. 2R-1; after the wait a __syncwarp makes the whole slot
-// visible and each thread reads its copy's four values transposed.
+// with E00 = sum v0 s0, E11 = sum v1 s1 and the cross sum KE = sum v0 s1 + v1 s0 = QE - E00 - E11,
+// QE = sum (v0 + v1)(s0 + s1) (F.. and QF from rows 2, 3), and U.. the same over u0 = v0 + v2,
+// u1 = v1 + v3 and t0 = s0 + s2, t1 = s1 + s3.  Round 0's sums (poly_eval_at over the pairs
+// (4i, 4i+1), (4i+2, 4i+3), sumcheck_helper.hpp:68-102) are p0_0 = E00 + F22,
+// p1_0 = E11 + F33 and p2raw_0 = QE + QF.  One pass over v therefore yields both rounds: the
+// finisher writes round 0's evaluations (times v(rx), since h = v(rx) s) for the transcript
+// and the 9R canonical sums to `sums`, and k_p2_round1_fin evaluates round 1 from them once r
+// is known — round 1 never reads v.
+// One copy per thread: nine products per repetition and group, summed unreduced in 64-bit
+// sums that fold64 folds every fourth group (below 2^34 + 4 (p - 1)^2 < 2^64).  A warp
+// covers 32 consecutive copies of one row group and stages it kP01Stages - 1 groups ahead
+// with one 16-byte cp.async per thread (row wl / 8, copies 4 (wl % 8) ..), plus the group's
+// scalars (s0..s3) and (t0, t1, s0 + s1, s2 + s3) of each repetition from lanes 0 .. 2R-1;
+// after the wait a __syncwarp makes the whole slot visible and each thread reads its
+// copy's four values transposed.
 constexpr int kP01Stages = 8;
-constexpr int kP01Sums = 9;       // E00, E11, KE, F22, F33, KF, U00, U11, KU
+constexpr int kP01Sums = 9;       // E00, E11, QE, F22, F33, QF, U00, U11, QU
 constexpr int kP01WarpSlot = 608;  // bytes per warp and stage: 4 rows x 32 copies x 4 B + 6 x 16 B scalars
 
 struct P01Src {
     const uint32_t* v;     // the layer input, 4 ngroups rows
     const uint32_t* s[3];  // s_j: 4 ngroups scalars (s0..s3 of each group)
-    const uint32_t* t[3];  // (t0, t1, 0, 0) of each group: 4 ngroups scalars
+    const uint32_t* t[3];  // (t0, t1, s0 + s1, s2 + s3) of each group: 4 ngroups scalars
 };
 
 // Round 0's evaluations from the nine sums of each repetition, times v(rx); the sums are
@@ -973,8 +986,7 @@ struct P01Fin {
                 m[k] = take(red, kP01Sums * j + k, N, lane);
                 sums[(size_t)(kP01Sums * j + k) * N + lane] = m[k];
             }
-            const uint32_t p0 = add(m[0], m[3]), p1 = add(m[1], m[4]);
-            const uint32_t p2raw = add(add(p0, p1), add(m[2], m[5]));
+            const uint32_t p0 = add(m[0], m[3]), p1 = add(m[1], m[4]), p2raw = add(m[2], m[5]);
             const uint32_t x = vx[(size_t)j * N + lane];
             out[(size_t)(3 * j) * N + lane] = mul(p0, x);
             out[(size_t)(3 * j + 1) * N + lane] = mul(p1, x);
@@ -1029,41 +1041,24 @@ __global__ void __launch_bounds__(256, 2) k_p2_round01(P01Src src, uint64_t ngro
             const uint32_t* rows = reinterpret_cast<const uint32_t*>(st);
             const uint32_t x0 = rows[wl], x1 = rows[32 + wl], x2 = rows[64 + wl], x3 = rows[96 + wl];
             const uint4* sc = reinterpret_cast<const uint4*>(st + 512);
-            const uint32_t u0 = add(x0, x2), u1 = add(x1, x3);
+            const uint32_t u0 = add(x0, x2), u1 = add(x1, x3), w01 = add(x0, x1), w23 = add(x2, x3), wu = add(u0, u1);
 #pragma unroll
             for (int j = 0; j < R; j++) {
                 const uint4 sv = sc[2 * j], tv = sc[2 * j + 1];
                 uint64_t* a = acc + kP01Sums * j;
                 mad64(a[0], x0, sv.x);
                 mad64(a[1], x1, sv.y);
-                mad64(a[2], x0, sv.y);
-                mad64(a[2], x1, sv.x);
+                mad64(a[2], w01, tv.z);
                 mad64(a[3], x2, sv.z);
                 mad64(a[4], x3, sv.w);
-                mad64(a[5], x2, sv.w);
-                mad64(a[5], x3, sv.z);
+                mad64(a[5], w23, tv.w);
                 mad64(a[6], u0, tv.x);
                 mad64(a[7], u1, tv.y);
-                mad64(a[8], u0, tv.y);
-                mad64(a[8], u1, tv.x);
-            }
-            // a K sum gains two products per group, the others one: folding the K sums every
-            // second group and the others every fourth keeps each below 2^34 + 4 (p - 1)^2 < 2^64
-            if (it & 1) {
-#pragma unroll
-                for (int j = 0; j < R; j++) {
-                    acc[kP01Sums * j + 2] = fold64(acc[kP01Sums * j + 2]);
-                    acc[kP01Sums * j + 5] = fold64(acc[kP01Sums * j + 5]);
-                    acc[kP01Sums * j + 8] = fold64(acc[kP01Sums * j + 8]);
-                }
+                mad64(a[8], wu, add(tv.x, tv.y));
             }
             if ((it & 3) == 3) {
 #pragma unroll
-                for (int j = 0; j < R; j++) {
-#pragma unroll
-                    for (int k = 0; k < kP01Sums; k++)
-                        if (k % 3 != 2) acc[kP01Sums * j + k] = fold64(acc[kP01Sums * j + k]);
-                }
+                for (int c = 0; c < R * kP01Sums; c++) acc[c] = fold64(acc[c]);
             }
             slot = slot + 1 == kP01Stages ? 0 : slot + 1;
         }
@@ -1099,6 +1094,9 @@ __global__ void __launch_bounds__(256) k_p2_round1_fin(const uint32_t* __restric
                 uint32_t m[kP01Sums];
 #pragma unroll
                 for (int k = 0; k < kP01Sums; k++) m[k] = __ldg(sums + (size_t)(kP01Sums * j + k) * N + lane);
+                // the cross sums KE, KF, KU from QE, QF, QU
+#pragma unroll
+                for (int k = 2; k < kP01Sums; k += 3) m[k] = sub(sub(m[k], m[k - 2]), m[k - 1]);
                 const uint32_t p0 = add(add(mul(c0, m[0]), mul(c1, m[2])), mul(c2, m[1]));
                 const uint32_t p1 = add(add(mul(c0, m[3]), mul(c1, m[5])), mul(c2, m[4]));
                 const uint32_t p2raw = add(add(mul(c0, m[6]), mul(c1, m[8])), mul(c2, m[7]));
@@ -1149,8 +1147,8 @@ __global__ void k_s_build(uint64_t I, uint64_t O, const uint32_t* __restrict__ m
 }
 
 // k_s_build over groups of four rows (I a multiple of 4), one thread per group, which also
-// writes t_j(i) = (s_j(4i) + s_j(4i+2), s_j(4i+1) + s_j(4i+3), 0, 0), the scalar pair sums
-// that k_p2_round01 stages with each group.
+// writes t_j(i) = (s_j(4i) + s_j(4i+2), s_j(4i+1) + s_j(4i+3), s_j(4i) + s_j(4i+1),
+// s_j(4i+2) + s_j(4i+3)), the scalar pair sums that k_p2_round01 stages with each group.
 __global__ void k_s_build4(uint64_t I, uint64_t O, const uint32_t* __restrict__ my_off, const uint4* __restrict__ my_g,
                            const uint32_t* __restrict__ eqc, const uint32_t* __restrict__ eqrx, uint32_t* __restrict__ s_out,
                            uint32_t* __restrict__ t_out, uint64_t s_stride, uint32_t reps) {
@@ -1172,7 +1170,7 @@ __global__ void k_s_build4(uint64_t I, uint64_t O, const uint32_t* __restrict__ 
         for (uint32_t j = 0; j < reps; j++) {
             reinterpret_cast<uint4*>(s_out + (uint64_t)j * s_stride)[gi] = make_uint4(s[j][0], s[j][1], s[j][2], s[j][3]);
             reinterpret_cast<uint4*>(t_out + (uint64_t)j * s_stride)[gi] =
-                make_uint4(add(s[j][0], s[j][2]), add(s[j][1], s[j][3]), 0u, 0u);
+                make_uint4(add(s[j][0], s[j][2]), add(s[j][1], s[j][3]), add(s[j][0], s[j][1]), add(s[j][2], s[j][3]));
         }
     }
 }

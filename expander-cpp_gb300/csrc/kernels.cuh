@@ -142,8 +142,9 @@ uint32_t p2_round01_groups(uint32_t N);
 cudaError_t launch_p2_round1_fin(int reps, const uint32_t* sums, const uint32_t* vx, const uint32_t* const* s,
                                  uint32_t* const* sd, const uint32_t* r, uint64_t ngroups, uint32_t N,
                                  uint32_t* evals_out, unsigned int* done, cudaStream_t st);
-// launch_s_build plus the pair sums t_j(i) = (s_j(4i) + s_j(4i+2), s_j(4i+1) + s_j(4i+3), 0, 0)
-// into t_out (4 I/4 entries, stride s_stride); I and s_stride multiples of 4.
+// launch_s_build plus the pair sums t_j(i) = (s_j(4i) + s_j(4i+2), s_j(4i+1) + s_j(4i+3),
+// s_j(4i) + s_j(4i+1), s_j(4i+2) + s_j(4i+3)) into t_out (4 I/4 entries, stride s_stride);
+// I and s_stride multiples of 4.
 cudaError_t launch_s_build4(uint64_t I, uint64_t O, const uint32_t* my_off, const uint4* my_g, const uint32_t* eqc,
                             const uint32_t* eqrx, uint32_t* s_out, uint32_t* t_out, uint64_t s_stride, uint32_t reps,
                             cudaStream_t s);
