@@ -826,14 +826,20 @@ __global__ void __launch_bounds__(256) k_p2_round2(RoundPtrs p, uint64_t npairs,
     reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, vx, g.N, (uint32_t)R});
 }
 
-// x == x mod p with x < 2^34: x = hi 2^32 + lo and 2^32 == 2 (mod 2^31 - 1), so
-// lo + 2 hi < 3 * 2^32; two multiply-adds on the integer FMA pipe (lo + 2 hi with its carry,
-// then bit 31 of hi plus that carry).  After it, three more products <= (p - 1)^2 keep a
-// 64-bit sum below 2^34 + 3 * 2^62.
+// x == x mod p for any 64-bit x: x = hi 2^32 + lo and 2^32 == 2 (mod 2^31 - 1), so the result
+// lo + 2 hi < 3 * 2^32.  Formed with a shift and an add with carry on the integer ALU (the
+// multiply pipe is what the sum kernels saturate).  After it, four more products
+// <= (p - 1)^2 keep a 64-bit sum below 3 * 2^32 + 2^64 - 2^35 + 16 < 2^64.
 __device__ __forceinline__ uint64_t fold64(uint64_t x) {
-    uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32), nl, nh;
-    asm("mad.lo.cc.u32 %0, %2, 2, %3;\n\t"
-        "madc.hi.u32 %1, %2, 2, 0;"
+    const uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
+    uint32_t nl, nh;
+    asm("{\n\t"
+        ".reg .u32 t;\n\t"
+        "shl.b32 t, %2, 1;\n\t"
+        "add.cc.u32 %0, %3, t;\n\t"
+        "shr.u32 t, %2, 31;\n\t"
+        "addc.u32 %1, t, 0;\n\t"
+        "}"
         : "=r"(nl), "=r"(nh)
         : "r"(hi), "r"(lo));
     return ((uint64_t)nh << 32) | nl;
@@ -954,7 +960,7 @@ __global__ void __launch_bounds__(256, 2) k_p2_round0(P2Src src, uint64_t npairs
 // and the 9R canonical sums to `sums`, and k_p2_round1_fin evaluates round 1 from them once r
 // is known — round 1 never reads v.
 // One copy per thread: nine products per repetition and group, summed unreduced in 64-bit
-// sums that fold64 folds every fourth group (below 2^34 + 4 (p - 1)^2 < 2^64).  A warp
+// sums that fold64 folds every fourth group (below 3 * 2^32 + 4 (p - 1)^2 < 2^64).  A warp
 // covers 32 consecutive copies of one row group and stages it kP01Stages - 1 groups ahead
 // with one 16-byte cp.async per thread (row wl / 8, copies 4 (wl % 8) ..), plus the group's
 // scalars (s0..s3) and (t0, t1, s0 + s1, s2 + s3) of each repetition from lanes 0 .. 2R-1;
