@@ -9,7 +9,7 @@ SHA-256 transcript, RAW commitment.  The witness (1 GiB) and the per-layer table
 (~90 GiB) are far larger than L2, so no flush is needed between steps.
 
   value : proofs/s with the input already resident in HBM (gkrgpu_prove_submit with a
-          device input), 3 proofs in flight so the host SHA-256 of the next proofs' RAW
+          device input), 4 proofs in flight so the host SHA-256 of the next proofs' RAW
           commitments overlaps the device work of the current one; timed from the device
           end of the last warm-up proof to the device end of the last timed proof
   e2e   : the same through the C ABI from pinned host buffers (input H2D, claims and
@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--cpu-copies", type=int, default=8, help="copies per proof in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--depth", type=int, default=3, help="proofs in flight (host hashing overlaps device work)")
+    ap.add_argument("--depth", type=int, default=4, help="proofs in flight (host hashing overlaps device work)")
     ap.add_argument("--tile", default="", help="threads_per_row,block,ctas for every kernel (default: autotuned)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default row tiles")
     ap.add_argument("--workload", choices=["plain", "mixed", "serve", "bn254"], default="plain",

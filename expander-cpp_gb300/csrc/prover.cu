@@ -352,7 +352,9 @@ struct gkrgpu_ctx {
     std::deque<gkrgpu_job*> host_q, gpu_q;
     std::vector<std::thread> workers;
     std::vector<std::unique_ptr<Lane>> lanes;
-    int n_lanes = 1, host_workers = 2, running = 0;
+    // host stages (commitment hash, grinding) run on host_workers threads: the SHA-256 of a
+    // large commitment is sequential, so several proofs' hashes overlap each other
+    int n_lanes = 1, host_workers = 4, running = 0;
     int fs_hash = kFsSha256;  // transcript hash of jobs submitted from now on
     bool stopping = false;
 
@@ -1430,7 +1432,7 @@ int gkrgpu_set_concurrency(gkrgpu_ctx* ctx, int lanes, uint64_t hbm_budget_bytes
         DeviceGuard dg(ctx->device);
         if (lanes) {
             ctx->n_lanes = lanes;
-            ctx->host_workers = std::max(2, std::min(lanes, 8));
+            ctx->host_workers = std::max(4, std::min(lanes, 8));
         }
         if (hbm_budget_bytes) {
             ctx->hbm_budget = hbm_budget_bytes;

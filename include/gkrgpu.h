@@ -198,6 +198,8 @@ typedef struct gkrgpu_job gkrgpu_job;
  * already running (a proof larger than the budget runs alone).  Workspaces come from a
  * stream-ordered pool and are returned when the proof ends.  Waits for queued proofs
  * first; 0 keeps the current value (default budget: 90% of the free memory at creation).
+ * Host stages (the commitment's SHA-256 and grinding) run on max(4, min(lanes, 8)) host
+ * threads, so the sequential hashes of several queued proofs overlap.
  * No counterpart in the reference, which proves one circuit per thread. */
 int gkrgpu_set_concurrency(gkrgpu_ctx* ctx, int lanes, uint64_t hbm_budget_bytes);
 /* Device bytes one proof of this circuit holds while it runs. */
