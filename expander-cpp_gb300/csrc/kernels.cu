@@ -376,13 +376,13 @@ __device__ __forceinline__ void cp_async_wait() {
 // (k_hg_round1) rebuilds it, which costs the gathers again but saves writing and re-reading
 // R full-width tables.  All repetitions in one thread: each gathered v[y] row serves the R
 // weights.
-// The round reads 4 bytes per copy and row and is bound by integer instructions, so the
-// sums are kept as p0 = sum f0 h0, p1 = sum f1 h1 and the cross term pc = sum f0 h1 + f1 h0
-// (p2raw = sum (f0 + f1)(h0 + h1) = p0 + p1 + pc, formed by the finisher), each product
-// added with mac_lazy (no reduction to canonical form), h of one row live at a time; a row
-// without mul gates (most rows of a wide layer) takes hg_j = a_j directly.  The pair's two
-// input rows, their add-gate weights and CSR offsets are staged by cp.async kStages - 1
-// iterations ahead.
+// The round reads 4 bytes per copy and row and is bound by the integer multiply pipe, so
+// the sums p0 = sum f0 h0, p1 = sum f1 h1 and p2raw = sum (f0 + f1)(h0 + h1) take each product
+// unreduced below 2^32 (mac_lazy) with h of one row live at a time: a row adds f_s h to p_s
+// and (f0 + f1) h to p2raw.  A pair whose rows both lack mul gates (most pairs of a wide
+// layer) has the scalar add weights as h and costs three products per copy and repetition:
+// f0 a0, f1 a1 and (f0 + f1)(a0 + a1).  The pair's two input rows, their add-gate weights and
+// CSR offsets are staged by cp.async kStages - 1 iterations ahead.
 constexpr int kStages = 3;
 constexpr int kStageFields = 5;  // v(2i), v(2i+1), a(2i), a(2i+1), (off(2i), off(2i+1), off(2i+2))
 constexpr int kMaxStagedSmem = kStages * kStageFields * 16 * 256;
@@ -401,16 +401,18 @@ __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict
     for (int c = 0; c < 3 * R; c++)
 #pragma unroll
         for (int l = 0; l < 4; l++) acc[c][l] = 0u;
-    // row x of the pair (s = 0: x = 2i, s = 1: x = 2i+1): p_s += f_s h, pc += f_(1-s) h
+    // row x of the pair (s = 0: x = 2i, s = 1: x = 2i+1): p_s += f_s h, p2raw += (f0 + f1) h
     auto row = [&](int s, const uint4& fs, const uint4& fo, const uint4& a, uint32_t k0, uint32_t k1) {
         if (k0 == k1) {
 #pragma unroll
-            for (int j = 0; j < R; j++)
+            for (int l = 0; l < 4; l++) {
+                const uint32_t f01 = add(comp(fs, l), comp(fo, l));
 #pragma unroll
-                for (int l = 0; l < 4; l++) {
+                for (int j = 0; j < R; j++) {
                     acc[3 * j + s][l] = m31::mac_lazy(acc[3 * j + s][l], comp(fs, l), comp(a, j));
-                    acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], comp(fo, l), comp(a, j));
+                    acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], f01, comp(a, j));
                 }
+            }
             return;
         }
         uint32_t h[R][4];
@@ -428,13 +430,15 @@ __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict
                 for (int l = 0; l < 4; l++) h[j][l] = m31::mac_lazy(h[j][l], comp(vy, l), comp(w, j));
         }
 #pragma unroll
-        for (int j = 0; j < R; j++)
+        for (int l = 0; l < 4; l++) {
+            const uint32_t f01 = add(comp(fs, l), comp(fo, l));
 #pragma unroll
-            for (int l = 0; l < 4; l++) {
+            for (int j = 0; j < R; j++) {
                 const uint32_t hc = m31::from_u32(h[j][l]);
                 acc[3 * j + s][l] = m31::mac_lazy(acc[3 * j + s][l], comp(fs, l), hc);
-                acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], comp(fo, l), hc);
+                acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], f01, hc);
             }
+        }
     };
     if (t.active) {
         const uint64_t npairs = I >> 1, step = (uint64_t)gridDim.x * g.rps;
@@ -460,14 +464,30 @@ __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict
             cp_async_wait<kStages - 1>();
             const uint4* st = ring + (size_t)slot * kStageFields * B + tid;
             const uint4 f0 = st[0], f1 = st[B], off = st[4 * B];
-            row(0, f0, f1, st[2 * B], off.x, off.y);
-            row(1, f1, f0, st[3 * B], off.y, off.z);
+            if (off.x == off.z) {  // neither row has mul gates
+#pragma unroll
+                for (int j = 0; j < R; j++) {
+                    const uint32_t a0 = reinterpret_cast<const uint32_t*>(st + 2 * B)[j];
+                    const uint32_t a1 = reinterpret_cast<const uint32_t*>(st + 3 * B)[j];
+                    const uint32_t a01 = add(a0, a1);
+#pragma unroll
+                    for (int l = 0; l < 4; l++) {
+                        acc[3 * j][l] = m31::mac_lazy(acc[3 * j][l], comp(f0, l), a0);
+                        acc[3 * j + 1][l] = m31::mac_lazy(acc[3 * j + 1][l], comp(f1, l), a1);
+                        acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], add(comp(f0, l), comp(f1, l)), a01);
+                    }
+                }
+            } else {
+                row(0, f0, f1, st[2 * B], off.x, off.y);
+                row(1, f1, f0, st[3 * B], off.y, off.z);
+            }
             slot = slot + 1 == kStages ? 0 : slot + 1;
         }
         cp_async_wait<0>();
     }
-    __syncthreads();  // the ring is reused as the reduction's scratch
-    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R, true});
+    __syncthreads();  // the ring is reused as the reduction's scratch (sums below 2^32 are
+                      // added as they are: the finisher reduces the 64-bit totals)
+    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R});
 }
 
 // ---------------------------------------------------------------- phase one, round 1
