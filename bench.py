@@ -9,9 +9,12 @@ SHA-256 transcript, RAW commitment.  The witness (1 GiB) and the per-layer table
 (~90 GiB) are far larger than L2, so no flush is needed between steps.
 
   value : proofs/s with the input already resident in HBM (gkrgpu_prove_submit with a
-          device input), 4 proofs in flight so the host SHA-256 of the next proofs' RAW
-          commitments overlaps the device work of the current one; timed from the device
-          end of the last warm-up proof to the device end of the last timed proof
+          device input), 6 proofs in flight so the host SHA-256 of the next proofs' RAW
+          commitments overlaps the device work of the current ones, and two device lanes,
+          so two proofs' device stages overlap (one proof's host round trips and
+          integer-bound kernels leave HBM idle that the other proof's kernels use); timed
+          from the device end of the last warm-up proof to the last device end among the
+          timed proofs
   e2e   : the same through the C ABI from pinned host buffers (input H2D, claims and
           round rows D2H inside every step)
   roofline: the kernel with the largest device time; achieved = its algorithmic bytes per
@@ -54,7 +57,7 @@ def parse():
     ap.add_argument("--cpu-copies", type=int, default=8, help="copies per proof in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--depth", type=int, default=4, help="proofs in flight (host hashing overlaps device work)")
+    ap.add_argument("--depth", type=int, default=6, help="proofs in flight (host hashing overlaps device work)")
     ap.add_argument("--tile", default="", help="threads_per_row,block,ctas for every kernel (default: autotuned)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default row tiles")
     ap.add_argument("--workload", choices=["plain", "mixed", "serve", "bn254"], default="plain",
@@ -64,9 +67,9 @@ def parse():
                          "64 proofs batched")
     ap.add_argument("--proofs", type=int, default=512, help="mixed/serve: number of distinct proofs")
     ap.add_argument("--lanes", type=int, default=16, help="mixed/serve: proofs whose device stages overlap")
-    ap.add_argument("--plain-lanes", type=int, default=1,
+    ap.add_argument("--plain-lanes", type=int, default=2,
                     help="plain: proofs whose device stages overlap (one proof's per-round host round trips "
-                         "leave the device idle unless another proof's kernels fill them)")
+                         "and integer-bound kernels leave HBM idle unless another proof's kernels fill it)")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="mixed/serve: device-memory admission budget")
     ap.add_argument("--rates", default="200,500,1000,2000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=4.0, help="serve: seconds of arrivals per rate")
@@ -270,7 +273,9 @@ def pipelined(ctx, n_warm, n_timed, bufs, submit):
         if i + depth < total:
             sub(i + depth)
     stats1 = ctx.kernel_stats()
-    total_ms = ctx.elapsed_ms(0, n_timed)
+    # with several device lanes proofs may finish out of order: the region ends at the last
+    # timed proof's end, so every timed proof completes inside it
+    total_ms = max(ctx.elapsed_ms(0, k) for k in range(1, n_timed + 1))
     steps = [ctx.elapsed_ms(k, k + 1) for k in range(n_timed)]
     return total_ms, steps, [l for i, l in lat if i >= n_warm], stats0, stats1
 
@@ -315,8 +320,10 @@ def run_ours(args, D):
                             for k, v in tiles.items() if v["ms"] > 0}}
         ctx.reset_stats()
 
-    # ---- value: input resident in HBM
-    ctx.set_timing(True)
+    # ---- value: input resident in HBM.  Per-launch CUDA events are kept only with one lane:
+    # with two, another proof's kernels share the GPU and a launch's time is not its own
+    one_lane = args.plain_lanes <= 1
+    ctx.set_timing(one_lane)
     clocks = ClockSampler(device)
     clocks.start()
     D.barrier()
@@ -326,8 +333,7 @@ def run_ours(args, D):
     D.barrier()
     clk = clocks.stop()
     ctx.set_timing(False)
-    stats = stats_delta(s0, s1)
-    launches = int(sum(s["launches"] for s in stats.values()))
+    stats, stat_steps = stats_delta(s0, s1), args.steps
     max_ms = D.max(total_ms)
     value = D.world * args.steps / (max_ms / 1000.0)
     tail = [bytes(b[0][plen - 4096:plen]) for b in bufs[:min(depth, args.warmup + args.steps)]]
@@ -338,11 +344,12 @@ def run_ours(args, D):
     if not args.no_e2e:
         h0 = ctx.transfer_stats()
         D.barrier()
+        e2e_warm = max(1, args.warmup)
         e2e_ms, e2e_steps, e2e_lat, _, _ = pipelined(
-            ctx, 1, args.steps, bufs, lambda b, m: ctx.submit(dc, witness, b[0], b[1], marker=m))
+            ctx, e2e_warm, args.steps, bufs, lambda b, m: ctx.submit(dc, witness, b[0], b[1], marker=m))
         e2e_ms = D.max(e2e_ms)
         h1 = ctx.transfer_stats()
-        n_jobs = 1 + args.steps
+        n_jobs = e2e_warm + args.steps
         e2e = {"value": D.world * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
                "h2d_bytes_per_step": (h1[0] - h0[0]) // n_jobs, "d2h_bytes_per_step": (h1[1] - h0[1]) // n_jobs,
                "ms_per_step": e2e_ms / args.steps,
@@ -350,6 +357,22 @@ def run_ours(args, D):
                "note": f"gkrgpu_prove_submit/wait from pinned host memory, {depth} proofs in flight; the RAW "
                        "commitment is copied and hashed on the host from the input"}
         assert bytes(bufs[0][0][plen - 4096:plen]) == tail[0], "e2e proof differs from the device-input proof"
+
+    # ---- kernel times: with several lanes, a one-lane pass of two proofs after the timed regions
+    kernel_timing = "per-launch CUDA events on the library's stream inside the timed region"
+    if not one_lane:
+        ctx.set_concurrency(lanes=1)
+        ctx.set_timing(True)
+        kp_steps = 2
+        _, _, _, k0, k1 = pipelined(ctx, 1, kp_steps, bufs,
+                                    lambda b, m: ctx.submit(dc, None, b[0], b[1], d_input=din.ptr, marker=m))
+        ctx.set_timing(False)
+        stats, stat_steps = stats_delta(k0, k1), kp_steps
+        kernel_timing = (f"per-launch CUDA events in a one-lane pass of {kp_steps} proofs after the timed regions "
+                         f"(with {args.plain_lanes} lanes another proof's kernels share the GPU, so a launch's time "
+                         "there is not its own)")
+    launches_per_proof = sum(s["launches"] for s in stats.values()) / stat_steps
+    launches = int(round(launches_per_proof * args.steps))
 
     # ---- roofline of the dominant kernel
     peak, peak_kind = peaks()
@@ -367,9 +390,9 @@ def run_ours(args, D):
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": per_launch_bytes, "launches": s["launches"],
                 "ms_per_launch": per_launch_ms}
-    total_bytes = sum(v["bytes"] for v in stats.values()) / args.steps
-    kernel_ms = sum(v["ms"] for v in stats.values()) / args.steps
-    kernels = {k: {"launches_per_step": v["launches"] / args.steps, "ms_per_step": v["ms"] / args.steps,
+    total_bytes = sum(v["bytes"] for v in stats.values()) / stat_steps
+    kernel_ms = sum(v["ms"] for v in stats.values()) / stat_steps
+    kernels = {k: {"launches_per_step": v["launches"] / stat_steps, "ms_per_step": v["ms"] / stat_steps,
                    "GBps": (v["bytes"] / (v["ms"] / 1000.0) / 1e9) if v["ms"] else None}
                for k, v in stats.items() if v["launches"]}
 
@@ -383,17 +406,18 @@ def run_ours(args, D):
                 "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
                 "config": dict(cfg, parallelism=f"replicas x{D.world}" if D.world > 1 else "single",
-                               pipeline=f"{depth} proofs in flight; timed region = device end of the last warm-up "
-                                        "proof to device end of the last timed proof"),
+                               pipeline=f"{depth} proofs in flight, {args.plain_lanes} device lane(s) (that many "
+                                        "proofs' device stages overlap); timed region = device end of the last "
+                                        "warm-up proof to the last device end among the timed proofs"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "autotune": tiles,
                 "clocks": clk,
                 "latency_ms": {"p50": statistics.median(lat_ms), "p99": float(np.percentile(lat_ms, 99)),
-                               "device_ms_per_proof": step_ms},
+                               "device_end_intervals_ms": step_ms},
                 "hbm": {"algorithmic_bytes_per_proof": total_bytes,
                         "GBps_over_step": total_bytes / (max_ms / args.steps / 1000.0) / 1e9,
                         "GBps_over_kernels": total_bytes / (kernel_ms / 1000.0) / 1e9,
                         "kernel_ms_per_step": kernel_ms},
-                "kernels": kernels, "proof_bytes": plen}
+                "kernels": kernels, "kernel_timing": kernel_timing, "proof_bytes": plen}
         print(json.dumps(line), flush=True)
 
 
