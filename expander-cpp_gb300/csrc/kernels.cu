@@ -561,7 +561,8 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
                     uint32_t f[4];
 #pragma unroll
                     for (int l = 0; l < 4; l++) f[l] = fold(comp(v0, l), comp(v1, l), p.r[j]);
-                    st4(p.fdst[j], 2 * i + s, g.N, t.lane0, mk4(f));
+                    // null: round 2 refolds the layer input instead of reading stored copies
+                    if (p.fdst[0]) st4(p.fdst[j], 2 * i + s, g.N, t.lane0, mk4(f));
                     // a copy-independent hg row is recomputed by round 2 (k_round with H1)
                     if (off[2 * s] != off[2 * s + 2]) st4(p.hdst[j], 2 * i + s, g.N, t.lane0, mk4(h[j]));
 #pragma unroll
@@ -595,7 +596,10 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
 // rows q 2^HR .. (q+1) 2^HR - 1; where none of them has mul gates the previous round did
 // not store it, and it is recomputed by folding their add weights a_j at the challenges of
 // rounds 0 .. HR-1.  Round 2 (HR = 1) does not store its own output rows of that kind.
-template <bool SHARED, bool LANE_HG, bool FOLD, int HR = 0>
+// VREF (phase-one round 2 after a round 1 that stored no folded copies): the f source rows
+// 4i..4i+3 are refolded from the layer input p.fsrc[j] = v, rows 8i..8i+7 in pairs at the
+// round-0 challenge p.hr[0][j].
+template <bool SHARED, bool LANE_HG, bool FOLD, int HR = 0, bool VREF = false>
 __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx, Geo g,
                                                uint32_t reps, RedScratch red, uint32_t* evals_out) {
     const TileIdx t = tile_idx(g);
@@ -644,8 +648,18 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, con
             uint32_t f0[4], f1[4], h0[4], h1[4];
             if (FOLD) {
                 uint4 a[4];
+                if (VREF) {
+                    const uint32_t rv = j == 0 ? p.hr[0][0] : (j == 1 ? p.hr[0][1] : p.hr[0][2]);
 #pragma unroll
-                for (int k = 0; k < 4; k++) a[k] = ld4(fs, 4 * i + k, g.N, t.lane0);
+                    for (int k = 0; k < 4; k++) {
+                        const uint4 x0 = ld4(fs, 8 * i + 2 * k, g.N, t.lane0), x1 = ld4(fs, 8 * i + 2 * k + 1, g.N, t.lane0);
+                        a[k] = make_uint4(fold(x0.x, x1.x, rv), fold(x0.y, x1.y, rv), fold(x0.z, x1.z, rv),
+                                          fold(x0.w, x1.w, rv));
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) a[k] = ld4(fs, 4 * i + k, g.N, t.lane0);
+                }
                 if (LANE_HG) {
                     uint4 b[4];
                     bool keep0 = true, keep1 = true;  // store output rows 2i, 2i+1
@@ -1420,10 +1434,13 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, co
 }
 
 cudaError_t launch_round_hr(int round, int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
-                            uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
+                            uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s, bool refold_input) {
     if (reps < 1 || reps > 3 || !p.hoff || !p.ha || (round != 2 && round != 3)) return cudaErrorInvalidValue;
+    if (refold_input && round != 2) return cudaErrorInvalidValue;
     LaunchShape sh = rep_shape(g, npairs, block, ctas, reps);
-    if (round == 2)
+    if (round == 2 && refold_input)
+        k_round<false, true, true, 1, true><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
+    else if (round == 2)
         k_round<false, true, true, 1><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
     else
         k_round<false, true, true, 2><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);

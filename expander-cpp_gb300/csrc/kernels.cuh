@@ -109,15 +109,18 @@ cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint
                              const uint4* a4, const uint4* w4, const Geo& g, uint32_t block, uint32_t ctas,
                              RedScratch red, uint32_t* evals_out, cudaStream_t s);
 // Phase-one round 1 rebuilding hg from the gate weights (no stored hg table): outputs
-// p.fdst[j] / p.hdst[j] (I/2 rows each), challenges p.r[j]; npairs = I/4.
+// p.fdst[j] / p.hdst[j] (I/2 rows each; p.fdst[0] null: the folded copies are not stored),
+// challenges p.r[j]; npairs = I/4.
 cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* mx_off, const uint4* mx_g,
                              const uint4* a4, const uint4* w4, const RoundPtrs& p, const Geo& g, uint32_t block,
                              uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
 // Phase-one round 2 or 3 (k = round, a k_round with per-copy hg and fold) reading the
 // previous round's stored hg rows and recomputing the copy-independent ones (p.hoff, p.ha,
-// p.hr); round 2 in turn does not store its copy-independent output rows.
+// p.hr); round 2 in turn does not store its copy-independent output rows.  With
+// refold_input (round 2 only) the f rows are refolded from the layer input p.fsrc[j] at the
+// round-0 challenges p.hr[0][j] (round 1 stored no folded copies).
 cudaError_t launch_round_hr(int round, int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
-                            uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
+                            uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s, bool refold_input);
 // Phase-two round 2 refolding the layer input p.fsrc[0] at the round-0 challenges p.hr[0]
 // (round 1 stored only its scalar tables) and at p.r; outputs p.fdst / p.hdst as k_round.
 cudaError_t launch_p2_round2(int reps, const RoundPtrs& p, uint64_t npairs, const uint32_t* vx, const Geo& g,

@@ -887,10 +887,16 @@ struct Prover {
             const double S = 4.0 * npairs;
             c.tag = ((uint32_t)li << 16) | (1u << 8) | k;
             int kid = K_ROUND_LANE;
+            // with a round 2, round 1 stores no folded copies of the layer input (they would be
+            // written once and read once): round 2 refolds v at the round-0 challenges
+            const bool refold1 = n >= 3;
             if (k == 1) {
                 // hg rebuilt from the weights: v read once, the gathers again, f and hg halves out
                 kid = K_HG_ROUND1;
-                c.launch(K_HG_ROUND1, rb * (I + Ly.nmul + (double)R * I - (double)R * Ly.h1_scalar_rows) + 32.0 * Ly.nmul + 20.0 * I, [&] {
+                if (refold1)
+                    for (int j = 0; j < R; j++) p.fdst[j] = nullptr;
+                const double f_out = refold1 ? 0.0 : (double)R * I / 2;
+                c.launch(K_HG_ROUND1, rb * (I + Ly.nmul + f_out + (double)R * I / 2 - (double)R * Ly.h1_scalar_rows) + 32.0 * Ly.nmul + 20.0 * I, [&] {
                     return launch_hg_round1(R, v, npairs, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, p, gk[K_HG_ROUND1],
                                             X.block, ck_ctas[K_HG_ROUND1], red_mapped(), c.evals_d(), c.stream);
                 });
@@ -907,10 +913,16 @@ struct Prover {
                 const double in_sc = (double)R * (k == 2 ? Ly.h1_scalar_rows : Ly.h2_scalar_rows);
                 const double out_sc = k == 2 ? (double)R * Ly.h2_scalar_rows : 0.0;
                 const double span = k == 2 ? 2.0 : 4.0;
-                const double hb2 = rb * (3.0 * R * S - in_sc - out_sc) + in_sc * 16.0 * span + 20.0 * npairs * R;
+                const bool vref = k == 2 && refold1;
+                if (vref)
+                    for (int j = 0; j < R; j++) p.fsrc[j] = v;
+                // f rows read: R S stored copies, or the 2 S input rows they fold (shared by the
+                // repetitions' CTAs through L2)
+                const double f_in = vref ? 2.0 * S : (double)R * S;
+                const double hb2 = rb * (f_in + 2.0 * R * S - in_sc - out_sc) + in_sc * 16.0 * span + 20.0 * npairs * R;
                 c.launch(K_ROUND_LANE, hb2, [&] {
                     return launch_round_hr((int)k, R, p, npairs, gk[K_ROUND_LANE], X.block, ck_ctas[K_ROUND_LANE],
-                                           red_mapped(), c.evals_d(), c.stream);
+                                           red_mapped(), c.evals_d(), c.stream, vref);
                 });
             } else {
                 c.launch(K_ROUND_LANE, rb * 3.0 * R * S, [&] {

@@ -48,6 +48,8 @@ def test_gpu_evaluate_matches_reference_golden(ctx, name):
 @pytest.mark.parametrize("seed,widths,n", [
     (201, [9, 11, 9, 11], 64), (202, [12, 10, 12], 16), (203, [8, 8, 8, 8, 8, 8], 128),
     (204, [2, 9, 3, 10, 1], 32), (205, [13, 11], 8), (206, [10, 12, 10], 1024),
+    # row slices of 96 and 160 copies: the one-copy-per-thread kernels leave warps idle
+    (207, [9, 10, 9], 96), (208, [8, 9, 8], 160),
 ])
 def test_gpu_matches_oracle_random(ctx, oracle, seed, widths, n):
     circ = gc.random_circuit(seed, widths, p_mul=0.6, p_local=0.8, window=256)
