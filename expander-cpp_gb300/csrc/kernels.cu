@@ -337,13 +337,15 @@ struct CopyFin {
     }
 };
 
+// p0 += f0 h0, p1 += f1 h1, p2raw += (f0 + f1)(h0 + h1) for four copies, each product added
+// unreduced below 2^32 (mac_lazy): the reduction's 64-bit totals are reduced by the finisher.
 __device__ __forceinline__ void accum_pair(uint32_t (&acc)[3][4], const uint32_t (&f0)[4], const uint32_t (&f1)[4],
                                            const uint32_t (&h0)[4], const uint32_t (&h1)[4]) {
 #pragma unroll
     for (int l = 0; l < 4; l++) {
-        acc[0][l] = add(acc[0][l], mul(f0[l], h0[l]));
-        acc[1][l] = add(acc[1][l], mul(f1[l], h1[l]));
-        acc[2][l] = add(acc[2][l], mul(add(f0[l], f1[l]), add(h0[l], h1[l])));
+        acc[0][l] = m31::mac_lazy(acc[0][l], f0[l], h0[l]);
+        acc[1][l] = m31::mac_lazy(acc[1][l], f1[l], h1[l]);
+        acc[2][l] = m31::mac_lazy(acc[2][l], add(f0[l], f1[l]), add(h0[l], h1[l]));
     }
 }
 
