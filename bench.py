@@ -613,26 +613,41 @@ def run_bn254(args, D):
                             for k, v in tiles.items() if v["ms"] > 0}}
         ctx.reset_stats()
 
-    ctx.set_timing(True)
+    # plain proofs with args.plain_lanes device lanes; per-launch times from a one-lane pass
+    one_lane = args.plain_lanes <= 1
+    if not one_lane:
+        ctx.set_concurrency(lanes=args.plain_lanes)
+    ctx.set_timing(one_lane)
     clocks = ClockSampler(D.local_rank)
     clocks.start()
     total_ms, step_ms, lat_ms, s0, s1 = pipelined(
         ctx, args.warmup, args.steps, bufs, lambda b, m: ctx.submit(dc, None, b[0], b[1], d_input=din.ptr, marker=m))
     clk = clocks.stop()
     ctx.set_timing(False)
-    stats = stats_delta(s0, s1)
+    stats, stat_steps = stats_delta(s0, s1), args.steps
     value = args.steps / (total_ms / 1000.0)
     e2e = None
     if not args.no_e2e:
         h0 = ctx.transfer_stats()
-        e2e_ms, _, e2e_lat, _, _ = pipelined(ctx, 1, args.steps, bufs,
+        e2e_warm = max(1, args.warmup)
+        e2e_ms, _, e2e_lat, _, _ = pipelined(ctx, e2e_warm, args.steps, bufs,
                                             lambda b, m: ctx.submit(dc, witness, b[0], b[1], marker=m))
         h1 = ctx.transfer_stats()
-        n_jobs = 1 + args.steps
+        n_jobs = e2e_warm + args.steps
         e2e = {"value": args.steps / (e2e_ms / 1000.0), "unit": UNIT,
                "h2d_bytes_per_step": (h1[0] - h0[0]) // n_jobs, "d2h_bytes_per_step": (h1[1] - h0[1]) // n_jobs,
                "latency_ms": {"p50": statistics.median(e2e_lat), "p99": float(np.percentile(e2e_lat, 99))}}
-    kernels = {k: {"launches_per_step": v["launches"] / args.steps, "ms_per_step": v["ms"] / args.steps,
+    kernel_timing = "per-launch CUDA events on the library's stream inside the timed region"
+    if not one_lane:
+        ctx.set_concurrency(lanes=1)
+        ctx.set_timing(True)
+        _, _, _, k0, k1 = pipelined(ctx, 1, 2, bufs,
+                                    lambda b, m: ctx.submit(dc, None, b[0], b[1], d_input=din.ptr, marker=m))
+        ctx.set_timing(False)
+        stats, stat_steps = stats_delta(k0, k1), 2
+        kernel_timing = (f"per-launch CUDA events in a one-lane pass of 2 proofs after the timed regions (with "
+                         f"{args.plain_lanes} lanes another proof's kernels share the GPU)")
+    kernels = {k: {"launches_per_step": v["launches"] / stat_steps, "ms_per_step": v["ms"] / stat_steps,
                    "GBps": (v["bytes"] / (v["ms"] / 1000.0) / 1e9) if v["ms"] else None}
                for k, v in stats.items() if v["launches"]}
     peak, peak_kind = peaks()
@@ -695,12 +710,14 @@ def run_bn254(args, D):
                                    f"wiring, {N} copies, uniform witness in [0, r), SHA-256 transcript, RAW "
                                    "commitment (one plain proof per step)",
                        "n_copies": N, "layers": depth_l, "width_log2": width, "field": "BN254", "repetitions": 1,
-                       "grinding_bits": 10, "pipeline": f"{args.depth} proofs in flight"},
+                       "grinding_bits": 10,
+                       "pipeline": f"{args.depth} proofs in flight, {args.plain_lanes} device lane(s)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": int(sum(v["launches"] for v in stats.values())), "autotune": tiles, "clocks": clk,
+            "gpu_launches": int(round(sum(v["launches"] for v in stats.values()) / stat_steps * args.steps)),
+            "autotune": tiles, "clocks": clk,
             "latency_ms": {"p50": statistics.median(lat_ms), "p99": float(np.percentile(lat_ms, 99)),
-                           "device_ms_per_proof": step_ms},
-            "kernels": kernels, "proof_bytes": plen,
+                           "device_end_intervals_ms": step_ms},
+            "kernels": kernels, "kernel_timing": kernel_timing, "proof_bytes": plen,
             "batched": {"proofs": n_b, "widths_log2": sorted(set(int(k) for k in ks)), "layers": depth_l,
                         "n_copies": N, "lanes": args.lanes, "proofs_per_s": batch_v,
                         "latency_ms": {"p50": statistics.median(batch_lat),
