@@ -248,11 +248,11 @@ def run_reference(args, D):
 
 def pipelined(ctx, n_warm, n_timed, bufs, submit):
     """Runs n_warm + n_timed proofs keeping len(bufs) in flight (host stage of the next
-    proofs overlapping the device stage of the current one).  The timed region runs from
-    the device end of the last warm-up proof (marker 0) to the device end of the last timed
-    proof (marker n_timed): exactly n_timed proofs complete inside it.  Returns (total ms,
-    per-proof device ms between consecutive ends, per-proof submit-to-done latency ms,
-    kernel stats at the start and end of the timed region)."""
+    proofs overlapping the device stage of the current ones).  The timed region runs from
+    the device end of the last warm-up proof (marker 0) to the latest device end among the
+    timed proofs (markers 1..n_timed): every timed proof completes inside it.  Returns
+    (total ms, intervals between consecutive proof ends, per-proof submit-to-done latency ms,
+    kernel stats when the last warm-up proof and the last proof were waited for)."""
     depth = len(bufs)
     total = n_warm + n_timed
     jobs, t_sub, lat = {}, {}, []
