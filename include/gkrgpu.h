@@ -253,7 +253,9 @@ int gkrgpu_memcpy_d2h(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t byte
  * other call) finishes, so gkrgpu_kernel_stats, which may be called while proofs are in
  * flight, always reads whole proofs; it fills up to cap entries (one per kernel kind) and
  * returns how many kinds exist.  gkrgpu_set_timing and gkrgpu_reset_stats first wait for
- * queued proofs to finish. */
+ * queued proofs to finish.  When the environment variable GKRGPU_TRACE names a file at
+ * gkrgpu_create, every timed launch also appends a CSV line to it: kernel kind, layer,
+ * phase (0 evaluate, 1, 2), round, algorithmic bytes, milliseconds. */
 int gkrgpu_set_timing(gkrgpu_ctx* ctx, int enabled);
 int gkrgpu_reset_stats(gkrgpu_ctx* ctx);
 int gkrgpu_kernel_stats(gkrgpu_ctx* ctx, gkrgpu_kernel_stat* out, int cap);
