@@ -7,17 +7,23 @@
 // arrays of u32 read by broadcast.
 //
 // Reference counterparts:
-//   k_evaluate     CircuitLayer::evaluate                     include/circuit/circuit.hpp:92-105
-//   k_eq           _eq_evals_at                               include/LinearGKR/sumcheck_common.hpp:17-53
-//   k_weights      the scalar factors of _prepare_g_x_vals    include/LinearGKR/sumcheck_helper.hpp:188-229
-//   k_hg_round0    _prepare_g_x_vals + poly_eval_at(0)        sumcheck_helper.hpp:172-231, 68-102
-//   k_round        receive_challenge + poly_eval_at(k)        sumcheck_helper.hpp:104-133, 68-102
-//   k_s_build      _prepare_h_y_vals (copy-independent part)  sumcheck_helper.hpp:233-261
-//   k_wsum         eval_multilinear via an eq table           include/poly_commit/poly.hpp:88-104
+//   k_evaluate       CircuitLayer::evaluate                     include/circuit/circuit.hpp:92-105
+//   k_eq             _eq_evals_at                               include/LinearGKR/sumcheck_common.hpp:17-53
+//   k_weights        the scalar factors of _prepare_g_x_vals    include/LinearGKR/sumcheck_helper.hpp:188-229
+//   k_hg_round0      _prepare_g_x_vals + poly_eval_at(0)        sumcheck_helper.hpp:172-231, 68-102
+//   k_hg_round1      hg rebuilt + receive_challenge + poly_eval_at(1)
+//   k_round          receive_challenge + poly_eval_at(k)        sumcheck_helper.hpp:104-133, 68-102
+//   k_s_build(4)     _prepare_h_y_vals (copy-independent part)  sumcheck_helper.hpp:233-261
+//   k_p2_round01     phase-two poly_eval_at of rounds 0 and 1 from one pass (round 1's sums are
+//                    quadratic in round 0's challenge); k_p2_round1_fin finishes round 1
+//   k_p2_round2      phase-two round 2 refolding the layer input
+//   k_wsum           eval_multilinear via an eq table           include/poly_commit/poly.hpp:88-104
 //
-// The per-repetition kernels (k_hg_round0, k_round) give each CTA one repetition j =
-// blockIdx.x % R: the R CTAs of a row chunk are adjacent in launch order, run together and
-// share the layer input through L2, while each thread keeps only one repetition's state.
+// k_round gives each CTA one repetition j = blockIdx.x % R: the R CTAs of a row chunk are
+// adjacent in launch order, run together and share their common source rows through L2,
+// while each thread keeps only one repetition's state.  The kernels whose source is the
+// layer input itself (k_hg_round0/1, k_p2_round01, k_p2_round2) keep all R repetitions in a
+// thread, so each input row is read once.
 #include <atomic>
 
 #include "kernels.cuh"
