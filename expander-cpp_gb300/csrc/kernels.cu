@@ -604,10 +604,7 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
 // rows q 2^HR .. (q+1) 2^HR - 1; where none of them has mul gates the previous round did
 // not store it, and it is recomputed by folding their add weights a_j at the challenges of
 // rounds 0 .. HR-1.  Round 2 (HR = 1) does not store its own output rows of that kind.
-// VREF (phase-one round 2 after a round 1 that stored no folded copies): the f source rows
-// 4i..4i+3 are refolded from the layer input p.fsrc[j] = v, rows 8i..8i+7 in pairs at the
-// round-0 challenge p.hr[0][j].
-template <bool SHARED, bool LANE_HG, bool FOLD, int HR = 0, bool VREF = false>
+template <bool SHARED, bool LANE_HG, bool FOLD, int HR = 0>
 __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx, Geo g,
                                                uint32_t reps, RedScratch red, uint32_t* evals_out) {
     const TileIdx t = tile_idx(g);
@@ -656,18 +653,8 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, con
             uint32_t f0[4], f1[4], h0[4], h1[4];
             if (FOLD) {
                 uint4 a[4];
-                if (VREF) {
-                    const uint32_t rv = j == 0 ? p.hr[0][0] : (j == 1 ? p.hr[0][1] : p.hr[0][2]);
 #pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        const uint4 x0 = ld4(fs, 8 * i + 2 * k, g.N, t.lane0), x1 = ld4(fs, 8 * i + 2 * k + 1, g.N, t.lane0);
-                        a[k] = make_uint4(fold(x0.x, x1.x, rv), fold(x0.y, x1.y, rv), fold(x0.z, x1.z, rv),
-                                          fold(x0.w, x1.w, rv));
-                    }
-                } else {
-#pragma unroll
-                    for (int k = 0; k < 4; k++) a[k] = ld4(fs, 4 * i + k, g.N, t.lane0);
-                }
+                for (int k = 0; k < 4; k++) a[k] = ld4(fs, 4 * i + k, g.N, t.lane0);
                 if (LANE_HG) {
                     uint4 b[4];
                     bool keep0 = true, keep1 = true;  // store output rows 2i, 2i+1
@@ -738,6 +725,81 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, con
         }
     }
     reduce_group<3>(acc, g, t.active, red, 3 * j, RoundFin{red, evals_out, LANE_HG ? nullptr : vx, g.N, reps});
+}
+
+// Phase-one round 2 after a round 1 that stored no folded copies of the layer input, with
+// every repetition in one thread (each input row is loaded once for the R repetitions):
+// output row 2i + s (s = 0, 1) of f folds input rows 8i + 4s .. 8i + 4s + 3 in pairs at the
+// round-0 challenge r0_j (p.hr[0]) and then at the round-1 challenge r_j (p.r), and output
+// row 2i + s of hg folds round 1's hg rows 4i + 2s, 4i + 2s + 1 at r_j, a row round 1 did not
+// store (both its input rows without mul gates) being recomputed from the add weights at
+// r0_j (receive_challenge twice, sumcheck_helper.hpp:104-133).  Output hg rows whose four
+// input rows have no mul gates are not stored (round 3 recomputes them), as in
+// k_round<.., HR = 1>.
+template <int R>
+__global__ void __launch_bounds__(256) k_p1_round2(RoundPtrs p, uint64_t npairs, Geo g, RedScratch red,
+                                                   uint32_t* evals_out) {
+    const TileIdx t = tile_idx(g);
+    const uint32_t* __restrict__ v = p.fsrc[0];
+    uint32_t acc[3 * R][4];
+#pragma unroll
+    for (int c = 0; c < 3 * R; c++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[c][l] = 0u;
+    if (t.active) {
+        for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
+            // offsets of input rows 8i, 8i+2, .., 8i+8: round-1 hg row 4i + k covers input rows
+            // 8i + 2k, 8i + 2k + 1
+            uint32_t off[5];
+#pragma unroll
+            for (int k = 0; k <= 4; k++) off[k] = __ldg(p.hoff + 8 * i + 2 * k);
+            uint32_t fe[R][4], he[R][4];
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                const uint64_t q = 8 * i + 4 * s;
+                const uint4 x0 = ld4(v, q, g.N, t.lane0), x1 = ld4(v, q + 1, g.N, t.lane0);
+                const uint4 x2 = ld4(v, q + 2, g.N, t.lane0), x3 = ld4(v, q + 3, g.N, t.lane0);
+                const bool keep = off[2 * s] != off[2 * s + 2];
+#pragma unroll
+                for (int j = 0; j < R; j++) {
+                    const uint32_t r0 = p.hr[0][j], r1 = p.r[j];
+                    uint4 b[2];
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {
+                        const int k = 2 * s + e;
+                        if (off[k] == off[k + 1]) {
+                            const uint32_t* a = reinterpret_cast<const uint32_t*>(p.ha + (4 * i + k) * 2) + j;
+                            const uint32_t hv = fold(__ldg(a), __ldg(a + 4), r0);
+                            b[e] = make_uint4(hv, hv, hv, hv);
+                        } else {
+                            b[e] = ld4(p.hsrc[j], 4 * i + k, g.N, t.lane0);
+                        }
+                    }
+                    uint32_t f[4], h[4];
+#pragma unroll
+                    for (int l = 0; l < 4; l++) {
+                        f[l] = fold(fold(comp(x0, l), comp(x1, l), r0), fold(comp(x2, l), comp(x3, l), r0), r1);
+                        h[l] = fold(comp(b[0], l), comp(b[1], l), r1);
+                    }
+                    st4(p.fdst[j], 2 * i + s, g.N, t.lane0, mk4(f));
+                    if (keep) st4(p.hdst[j], 2 * i + s, g.N, t.lane0, mk4(h));
+#pragma unroll
+                    for (int l = 0; l < 4; l++) {
+                        if (s == 0) {
+                            acc[3 * j][l] = m31::mac_lazy(acc[3 * j][l], f[l], h[l]);
+                            fe[j][l] = f[l];
+                            he[j][l] = h[l];
+                        } else {
+                            acc[3 * j + 1][l] = m31::mac_lazy(acc[3 * j + 1][l], f[l], h[l]);
+                            acc[3 * j + 2][l] =
+                                m31::mac_lazy(acc[3 * j + 2][l], add(fe[j][l], f[l]), add(he[j][l], h[l]));
+                        }
+                    }
+                }
+            }
+        }
+    }
+    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R});
 }
 
 // Shared-source rounds (phase-1 round 1, phase-2 rounds 0 and 1) with every repetition in
@@ -1442,16 +1504,26 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, co
 }
 
 cudaError_t launch_round_hr(int round, int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
-                            uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s, bool refold_input) {
+                            uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
     if (reps < 1 || reps > 3 || !p.hoff || !p.ha || (round != 2 && round != 3)) return cudaErrorInvalidValue;
-    if (refold_input && round != 2) return cudaErrorInvalidValue;
     LaunchShape sh = rep_shape(g, npairs, block, ctas, reps);
-    if (round == 2 && refold_input)
-        k_round<false, true, true, 1, true><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
-    else if (round == 2)
+    if (round == 2)
         k_round<false, true, true, 1><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
     else
         k_round<false, true, true, 2><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_p1_round2(int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
+                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
+    if (!p.hoff || !p.ha) return cudaErrorInvalidValue;
+    LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
+    switch (reps) {
+        case 1: k_p1_round2<1><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, g, red, evals_out); break;
+        case 2: k_p1_round2<2><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, g, red, evals_out); break;
+        case 3: k_p1_round2<3><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, g, red, evals_out); break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

@@ -116,11 +116,14 @@ cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const
                              uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
 // Phase-one round 2 or 3 (k = round, a k_round with per-copy hg and fold) reading the
 // previous round's stored hg rows and recomputing the copy-independent ones (p.hoff, p.ha,
-// p.hr); round 2 in turn does not store its copy-independent output rows.  With
-// refold_input (round 2 only) the f rows are refolded from the layer input p.fsrc[j] at the
-// round-0 challenges p.hr[0][j] (round 1 stored no folded copies).
+// p.hr); round 2 in turn does not store its copy-independent output rows.
 cudaError_t launch_round_hr(int round, int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
-                            uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s, bool refold_input);
+                            uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
+// Phase-one round 2 refolding the layer input p.fsrc[0] at the round-0 challenges p.hr[0][j]
+// and p.r[j], all repetitions per thread (round 1 stored no folded copies); hg rows as
+// launch_round_hr(2, ..) (p.hsrc, p.hoff, p.ha); npairs = I/8.
+cudaError_t launch_p1_round2(int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
+                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
 // Phase-two round 2 refolding the layer input p.fsrc[0] at the round-0 challenges p.hr[0]
 // (round 1 stored only its scalar tables) and at p.r; outputs p.fdst / p.hdst as k_round.
 cudaError_t launch_p2_round2(int reps, const RoundPtrs& p, uint64_t npairs, const uint32_t* vx, const Geo& g,

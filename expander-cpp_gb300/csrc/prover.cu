@@ -916,13 +916,15 @@ struct Prover {
                 const bool vref = k == 2 && refold1;
                 if (vref)
                     for (int j = 0; j < R; j++) p.fsrc[j] = v;
-                // f rows read: R S stored copies, or the 2 S input rows they fold (shared by the
-                // repetitions' CTAs through L2)
+                // f rows read: R S stored copies, or the 2 S input rows they fold (k_p1_round2
+                // reads each once for the R repetitions)
                 const double f_in = vref ? 2.0 * S : (double)R * S;
                 const double hb2 = rb * (f_in + 2.0 * R * S - in_sc - out_sc) + in_sc * 16.0 * span + 20.0 * npairs * R;
                 c.launch(K_ROUND_LANE, hb2, [&] {
-                    return launch_round_hr((int)k, R, p, npairs, gk[K_ROUND_LANE], X.block, ck_ctas[K_ROUND_LANE],
-                                           red_mapped(), c.evals_d(), c.stream, vref);
+                    return vref ? launch_p1_round2(R, p, npairs, gk[K_ROUND_LANE], X.block, ck_ctas[K_ROUND_LANE],
+                                                   red_mapped(), c.evals_d(), c.stream)
+                                : launch_round_hr((int)k, R, p, npairs, gk[K_ROUND_LANE], X.block,
+                                                  ck_ctas[K_ROUND_LANE], red_mapped(), c.evals_d(), c.stream);
                 });
             } else {
                 c.launch(K_ROUND_LANE, rb * 3.0 * R * S, [&] {
