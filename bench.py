@@ -71,6 +71,7 @@ def parse():
                     help="plain: proofs whose device stages overlap (one proof's per-round host round trips "
                          "and integer-bound kernels leave HBM idle unless another proof's kernels fill it)")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="mixed/serve: device-memory admission budget")
+    ap.add_argument("--no-batched", action="store_true", help="bn254: only the plain proofs (no 64-proof batch)")
     ap.add_argument("--rates", default="200,500,1000,2000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=4.0, help="serve: seconds of arrivals per rate")
     return ap.parse_args()
@@ -670,39 +671,48 @@ def run_bn254(args, D):
                "sample": f"{threads} threads x 1 proof of the same circuit at {cn} copies (oracle/gkr_oracle_bn254.c, "
                          f"evaluate + prove), scaled by {cn}/{N} to {N}-copy proofs/s"}
 
-    # ---- batched: 64 independent proofs, widths 2^12..2^16
-    n_b = 64
-    st = gc.Stream(99)
-    ks = (12 + st.below(n_b, 5)).tolist()
-    with ThreadPoolExecutor(8) as ex:
-        circs = list(ex.map(lambda i: gc.uniform_circuit(5000 + i, depth_l, int(ks[i]), p_mul=0.5), range(n_b)))
-        wits = list(ex.map(lambda i: gc.random_witness_bn254(5000 + i, int(ks[i]), N), range(n_b)))
-    dcs = [ctx.load(c, "BN254") for c in circs]
-    pbs = [np.empty(d.proof_size(N), np.uint8) for d in dcs]
-    cbs = [np.empty((1, N, 4), np.uint64) for _ in range(n_b)]
+    batched = None
+    if not args.no_batched:
+        # ---- batched: 64 independent proofs, widths 2^12..2^16
+        n_b = 64
+        st = gc.Stream(99)
+        ks = (12 + st.below(n_b, 5)).tolist()
+        with ThreadPoolExecutor(8) as ex:
+            circs = list(ex.map(lambda i: gc.uniform_circuit(5000 + i, depth_l, int(ks[i]), p_mul=0.5), range(n_b)))
+            wits = list(ex.map(lambda i: gc.random_witness_bn254(5000 + i, int(ks[i]), N), range(n_b)))
+        dcs = [ctx.load(c, "BN254") for c in circs]
+        pbs = [np.empty(d.proof_size(N), np.uint8) for d in dcs]
+        cbs = [np.empty((1, N, 4), np.uint64) for _ in range(n_b)]
 
-    def run_all(lanes):
-        ctx.set_concurrency(lanes=lanes, hbm_budget_bytes=int(args.budget_gb * (1 << 30)))
-        for i in range(min(lanes, n_b)):
-            ctx.wait(ctx.submit(dcs[i], wits[i], pbs[i], cbs[i]))
-        lat = []
-        t0 = time.perf_counter()
-        if lanes == 1:
-            for i in range(n_b):
-                t1 = time.perf_counter()
+        def run_all(lanes):
+            ctx.set_concurrency(lanes=lanes, hbm_budget_bytes=int(args.budget_gb * (1 << 30)))
+            for i in range(min(lanes, n_b)):
                 ctx.wait(ctx.submit(dcs[i], wits[i], pbs[i], cbs[i]))
-                lat.append((time.perf_counter() - t1) * 1000.0)
-        else:
-            subs = [(time.perf_counter(), ctx.submit(dcs[i], wits[i], pbs[i], cbs[i])) for i in range(n_b)]
-            for t1, j in subs:
-                ctx.wait(j)
-                lat.append((time.perf_counter() - t1) * 1000.0)
-        sec = time.perf_counter() - t0
-        import hashlib
-        return n_b / sec, lat, [hashlib.sha256(p.tobytes()).hexdigest() for p in pbs]
+            lat = []
+            t0 = time.perf_counter()
+            if lanes == 1:
+                for i in range(n_b):
+                    t1 = time.perf_counter()
+                    ctx.wait(ctx.submit(dcs[i], wits[i], pbs[i], cbs[i]))
+                    lat.append((time.perf_counter() - t1) * 1000.0)
+            else:
+                subs = [(time.perf_counter(), ctx.submit(dcs[i], wits[i], pbs[i], cbs[i])) for i in range(n_b)]
+                for t1, j in subs:
+                    ctx.wait(j)
+                    lat.append((time.perf_counter() - t1) * 1000.0)
+            sec = time.perf_counter() - t0
+            import hashlib
+            return n_b / sec, lat, [hashlib.sha256(p.tobytes()).hexdigest() for p in pbs]
 
-    plain_v, plain_lat, plain_d = run_all(1)
-    batch_v, batch_lat, batch_d = run_all(args.lanes)
+        plain_v, plain_lat, plain_d = run_all(1)
+        batch_v, batch_lat, batch_d = run_all(args.lanes)
+        batched = {"proofs": n_b, "widths_log2": sorted(set(int(k) for k in ks)), "layers": depth_l,
+                   "n_copies": N, "lanes": args.lanes, "proofs_per_s": batch_v,
+                   "latency_ms": {"p50": statistics.median(batch_lat), "p99": float(np.percentile(batch_lat, 99))},
+                   "plain_proofs_per_s": plain_v,
+                   "plain_latency_ms": {"p50": statistics.median(plain_lat),
+                                        "p99": float(np.percentile(plain_lat, 99))},
+                   "batched_over_plain": batch_v / plain_v, "byte_identical_to_plain": batch_d == plain_d}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u256 (BN254 Montgomery, 8 x u32 limbs)", "data": "synthetic",
@@ -718,14 +728,7 @@ def run_bn254(args, D):
             "latency_ms": {"p50": statistics.median(lat_ms), "p99": float(np.percentile(lat_ms, 99)),
                            "device_end_intervals_ms": step_ms},
             "kernels": kernels, "kernel_timing": kernel_timing, "proof_bytes": plen,
-            "batched": {"proofs": n_b, "widths_log2": sorted(set(int(k) for k in ks)), "layers": depth_l,
-                        "n_copies": N, "lanes": args.lanes, "proofs_per_s": batch_v,
-                        "latency_ms": {"p50": statistics.median(batch_lat),
-                                       "p99": float(np.percentile(batch_lat, 99))},
-                        "plain_proofs_per_s": plain_v,
-                        "plain_latency_ms": {"p50": statistics.median(plain_lat),
-                                             "p99": float(np.percentile(plain_lat, 99))},
-                        "batched_over_plain": batch_v / plain_v, "byte_identical_to_plain": batch_d == plain_d}}
+            "batched": batched}
     print(json.dumps(line), flush=True)
 
 
