@@ -47,8 +47,8 @@ UNIT = "proofs/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--copies", type=int, default=1024)
     ap.add_argument("--layers", type=int, default=24)
@@ -71,7 +71,12 @@ def parse():
                     help="plain: proofs whose device stages overlap (one proof's per-round host round trips "
                          "and integer-bound kernels leave HBM idle unless another proof's kernels fill it)")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="mixed/serve: device-memory admission budget")
-    ap.add_argument("--no-batched", action="store_true", help="bn254: only the plain proofs (no 64-proof batch)")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="plain: no mixed batched-vs-plain object; bn254: only the plain proofs (no 64-proof batch)")
+    ap.add_argument("--batched-proofs", type=int, default=128,
+                    help="plain: proofs of the shortened mixed workload measured batched and one at a time")
+    ap.add_argument("--no-keccak", action="store_true", help="plain: skip the Keccak-256 transcript rate")
+    ap.add_argument("--no-parity", action="store_true", help="plain: skip the golden and verifier checks")
     ap.add_argument("--rates", default="200,500,1000,2000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=4.0, help="serve: seconds of arrivals per rate")
     return ap.parse_args()
@@ -187,7 +192,8 @@ def workload(args):
 
 def cpu_sample(circ, args, n_steps=1, warmup=0):
     """Times the CPU prover (all host cores, one proof per thread) on the workload's circuit at
-    args.cpu_copies copies; returns (1024-copy-equivalent proofs/s per step, info)."""
+    args.cpu_copies copies.  Returns (per-step values scaled to args.copies-copy proofs/s,
+    per-step measured seconds, info)."""
     from gkr_gb300 import circuit as gc
     from oracle.oracle import Oracle, Reference
     threads = len(os.sched_getaffinity(0))
@@ -214,14 +220,27 @@ def cpu_sample(circ, args, n_steps=1, warmup=0):
         kind = "port"
     for _ in range(warmup):
         run()
-    vals = []
+    vals, secs = [], []
     for _ in range(n_steps):
         dt = run()
+        secs.append(dt)
         vals.append(threads / dt * args.cpu_copies / args.copies)
     info = {"cores": threads, "kind": kind,
-            "sample": f"{threads} threads x 1 proof of the same circuit at {args.cpu_copies} copies "
-                      f"(evaluate + prove), scaled by {args.cpu_copies}/{args.copies} to {args.copies}-copy proofs/s"}
-    return vals, info
+            "sample": f"{threads} threads x 1 proof of the same circuit at {args.cpu_copies} copies (evaluate + prove, "
+                      f"{statistics.mean(secs):.2f} s per sample), reported as {args.copies}-copy proofs/s: "
+                      f"{threads} proofs x {args.cpu_copies}/{args.copies} per sample time",
+            "sample_seconds": secs}
+    if kind == "port":
+        info["port_vs_reference"] = PORT_VS_REFERENCE
+    return vals, secs, info
+
+
+# The oracle port against the compiled reference (VectorizedM31, AVX-512) on the same
+# 8-copy proof of this circuit, one thread each, measured on an x86-64 host where both
+# build; the Arm GPU host has no reference tree, so there the port stands in for it.
+PORT_VS_REFERENCE = {"port_s": 12.2, "reference_s": 6.1, "ratio": 2.0,
+                     "note": "single-thread 8-copy config-2 proof on a Xeon with AVX-512; the port understates the "
+                             "reference's CPU speed by about this factor"}
 
 
 def peaks():
@@ -237,30 +256,46 @@ def run_reference(args, D):
     if D.rank != 0:
         return
     circ, widths, cfg = workload(args)
-    vals, info = cpu_sample(circ, args, n_steps=args.steps, warmup=args.warmup)
+    vals, secs, info = cpu_sample(circ, args, n_steps=args.steps, warmup=args.warmup)
     v = statistics.mean(vals)
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u32", "data": "synthetic", "config": cfg, "impl": "reference",
+            "warmup": args.warmup, "ms_per_step": 1000.0 * statistics.mean(secs), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic", "config": cfg,
+            "impl": "reference",
+            "value_kind": f"scaled sample: each step proves {info['cores']} proofs at {args.cpu_copies} copies on "
+                          f"{info['cores']} threads; value = {info['cores']} x {args.cpu_copies}/{args.copies} / "
+                          "step seconds; ms_per_step is the measured step time",
             "cpu_baseline": dict(info, value=v, unit=UNIT),
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
+# Timing-marker slots (gkrgpu_elapsed_ms): proofs submitted with marker k record their
+# device-stage end in slot k and its beginning in slot 64 + k; slot 63 is the reference
+# mark taken before any proof of a pipelined run is submitted.
+REF_SLOT = 63
+MAX_TIMED = 62
+
+
 def pipelined(ctx, n_warm, n_timed, bufs, submit):
     """Runs n_warm + n_timed proofs keeping len(bufs) in flight (host stage of the next
     proofs overlapping the device stage of the current ones).  The timed region runs from
-    the device end of the last warm-up proof (marker 0) to the latest device end among the
-    timed proofs (markers 1..n_timed): every timed proof completes inside it.  Returns
-    (total ms, intervals between consecutive proof ends, per-proof submit-to-done latency ms,
-    kernel stats when the last warm-up proof and the last proof were waited for)."""
+    the earliest device-stage beginning among the timed proofs to the latest device-stage
+    end among them, so it holds the whole device stage of every timed proof (and possibly
+    the tail of a warm-up proof on another lane, which is not counted).  Returns (total ms,
+    intervals between consecutive timed proof ends starting at the region's start,
+    per-proof submit-to-done latency ms, kernel stats when the last warm-up proof and the
+    last proof were waited for, per-proof device-stage ms)."""
+    if n_timed > MAX_TIMED:
+        raise ValueError(f"at most {MAX_TIMED} timed proofs per run")
     depth = len(bufs)
     total = n_warm + n_timed
     jobs, t_sub, lat = {}, {}, []
     stats0 = None
+    ctx.mark(REF_SLOT)
 
     def sub(i):
-        marker = i - (n_warm - 1) if i >= n_warm - 1 else -1
+        marker = i - n_warm if i >= n_warm else -1
         t_sub[i] = time.perf_counter()
         jobs[i] = submit(bufs[i % depth], marker)
 
@@ -273,24 +308,82 @@ def pipelined(ctx, n_warm, n_timed, bufs, submit):
             stats0 = ctx.kernel_stats()
         if i + depth < total:
             sub(i + depth)
+    if stats0 is None:
+        stats0 = {k: {"launches": 0, "ms": 0.0, "bytes": 0.0} for k in ctx.kernel_stats()}
     stats1 = ctx.kernel_stats()
-    # with several device lanes proofs may finish out of order: the region ends at the last
-    # timed proof's end, so every timed proof completes inside it
-    total_ms = max(ctx.elapsed_ms(0, k) for k in range(1, n_timed + 1))
-    steps = [ctx.elapsed_ms(k, k + 1) for k in range(n_timed)]
-    return total_ms, steps, [l for i, l in lat if i >= n_warm], stats0, stats1
+    begins = [ctx.elapsed_ms(REF_SLOT, 64 + k) for k in range(n_timed)]
+    ends = [ctx.elapsed_ms(REF_SLOT, k) for k in range(n_timed)]
+    t0, t1 = min(begins), max(ends)
+    e = sorted(ends)
+    steps = [b - a for a, b in zip([t0] + e[:-1], e)]
+    stage = [b - a for a, b in zip(begins, ends)]
+    return t1 - t0, steps, [l for i, l in lat if i >= n_warm], stats0, stats1, stage
 
 
 def stats_delta(s0, s1):
     return {k: {f: s1[k][f] - s0[k][f] for f in ("launches", "ms", "bytes")} for k in s1}
 
 
+def kernel_table(stats, n_steps, traffic_ratios):
+    """Per kernel kind: launches and device ms per step, the algorithmic-byte rate, and the
+    DRAM rate (algorithmic bytes x the ncu DRAM/algorithmic ratio of that kind, where one was
+    captured: gathers that hit L2 count as algorithmic bytes but not as DRAM traffic)."""
+    out = {}
+    for k, v in stats.items():
+        if not v["launches"]:
+            continue
+        alg = (v["bytes"] / (v["ms"] / 1000.0) / 1e9) if v["ms"] else None
+        r = traffic_ratios.get(k, {}).get("traffic_over_algorithmic")
+        out[k] = {"launches_per_step": v["launches"] / n_steps, "ms_per_step": v["ms"] / n_steps,
+                  "algorithmic_GBps": alg, "dram_GBps": alg * r if (alg and r) else None}
+    return out
+
+
+def roofline_of(stats, traffic_ratios):
+    """Roofline line of the kernel kind with the largest device time: its algorithmic bytes
+    per launch over its CUDA-event time per launch, against the measured HBM copy peak."""
+    peak, peak_kind = peaks()
+    name, s = max(stats.items(), key=lambda kv: kv[1]["ms"])
+    per_launch_bytes = s["bytes"] / max(s["launches"], 1)
+    per_launch_ms = s["ms"] / max(s["launches"], 1)
+    achieved = per_launch_bytes / (per_launch_ms / 1000.0) / 1e9 if per_launch_ms > 0 else 0.0
+    ratio = traffic_ratios.get(name, {}).get("traffic_over_algorithmic")
+    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": per_launch_bytes * ratio if ratio else None,
+            "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_launch_bytes, "launches": s["launches"],
+            "ms_per_launch": per_launch_ms}
+
+
+def load_traffic_ratios():
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    return json.load(open(tfile)) if os.path.exists(tfile) else {}
+
+
+def golden_parity(ctx, dc, circ, name="cfg2_n8"):
+    """Proves the benchmark circuit at the few copies of a golden case made by the compiled
+    reference (tests/golden/golden.json) and compares the digests of the proof and claims."""
+    import hashlib
+
+    from gkr_gb300 import circuit as gc
+    gfile = os.path.join(ROOT, "tests", "golden", "golden.json")
+    g = json.load(open(gfile)).get("large_cases", {}).get(name) if os.path.exists(gfile) else None
+    if g is None:
+        return {"case": name, "result": "no golden"}
+    w = gc.random_witness(g["witness_seed"], circ.log_input_size, g["n_copies"])
+    cv, proof = ctx.prove(dc, w, grinding_bits=g["grinding_bits"])
+    ok_p = hashlib.sha256(proof).hexdigest() == g["proof_sha256"] and len(proof) == g["proof_len"]
+    ok_c = hashlib.sha256(np.ascontiguousarray(cv).tobytes()).hexdigest() == g["claimed_v_sha256"]
+    return {"case": name, "n_copies": g["n_copies"], "proof_bytes": len(proof),
+            "result": "golden" if (ok_p and ok_c) else "MISMATCH",
+            "source": "digests of the compiled reference's proof of the same circuit and witness"}
+
+
 def run_ours(args, D):
     from gkr_gb300 import circuit as gc
     from gkr_gb300.prover import Context, DeviceBuffer, HostBuffer
 
-    if args.steps + 1 > 64:
-        raise SystemExit("--steps must be <= 63")
+    if args.steps > MAX_TIMED:
+        raise SystemExit(f"--steps must be <= {MAX_TIMED}")
     device = D.local_rank
     circ, widths, cfg = workload(args)
     N = args.copies
@@ -310,6 +403,7 @@ def run_ours(args, D):
     depth = args.depth
     pbufs = [HostBuffer(plen) for _ in range(depth)]
     bufs = [(pb.array, np.empty((3, N), np.uint32)) for pb in pbufs]
+    traffic = load_traffic_ratios()
 
     # row tiles from the autotuner (whole proofs timed per candidate; outside the timed region)
     tiles = None
@@ -321,6 +415,9 @@ def run_ours(args, D):
                             for k, v in tiles.items() if v["ms"] > 0}}
         ctx.reset_stats()
 
+    def dev_submit(b, m):
+        return ctx.submit(dc, None, b[0], b[1], d_input=din.ptr, marker=m)
+
     # ---- value: input resident in HBM.  Per-launch CUDA events are kept only with one lane:
     # with two, another proof's kernels share the GPU and a launch's time is not its own
     one_lane = args.plain_lanes <= 1
@@ -328,9 +425,7 @@ def run_ours(args, D):
     clocks = ClockSampler(device)
     clocks.start()
     D.barrier()
-    total_ms, step_ms, lat_ms, s0, s1 = pipelined(
-        ctx, args.warmup, args.steps, bufs,
-        lambda b, m: ctx.submit(dc, None, b[0], b[1], d_input=din.ptr, marker=m))
+    total_ms, step_ms, lat_ms, s0, s1, stage_ms = pipelined(ctx, args.warmup, args.steps, bufs, dev_submit)
     D.barrier()
     clk = clocks.stop()
     ctx.set_timing(False)
@@ -346,7 +441,7 @@ def run_ours(args, D):
         h0 = ctx.transfer_stats()
         D.barrier()
         e2e_warm = max(1, args.warmup)
-        e2e_ms, e2e_steps, e2e_lat, _, _ = pipelined(
+        e2e_ms, e2e_steps, e2e_lat, _, _, _ = pipelined(
             ctx, e2e_warm, args.steps, bufs, lambda b, m: ctx.submit(dc, witness, b[0], b[1], marker=m))
         e2e_ms = D.max(e2e_ms)
         h1 = ctx.transfer_stats()
@@ -359,47 +454,68 @@ def run_ours(args, D):
                        "commitment is copied and hashed on the host from the input"}
         assert bytes(bufs[0][0][plen - 4096:plen]) == tail[0], "e2e proof differs from the device-input proof"
 
-    # ---- kernel times: with several lanes, a one-lane pass of two proofs after the timed regions
+    # ---- the plain prover with one device lane (one proof's device stage at a time), then a
+    # short one-lane pass with per-launch CUDA events for the kernel table and roofline
+    plain1 = None
     kernel_timing = "per-launch CUDA events on the library's stream inside the timed region"
     if not one_lane:
         ctx.set_concurrency(lanes=1)
+        n1 = min(args.steps, 12)
+        p1_ms, _, p1_lat, _, _, p1_stage = pipelined(ctx, 2, n1, bufs[:4], dev_submit)
+        plain1 = {"proofs_per_s": n1 / (p1_ms / 1000.0), "ms_per_proof": p1_ms / n1, "steps": n1,
+                  "device_stage_ms_median": statistics.median(p1_stage),
+                  "note": "one device lane, 4 proofs in flight (host stages of the next proofs overlap), "
+                          "device input"}
         ctx.set_timing(True)
         kp_steps = 2
-        _, _, _, k0, k1 = pipelined(ctx, 1, kp_steps, bufs,
-                                    lambda b, m: ctx.submit(dc, None, b[0], b[1], d_input=din.ptr, marker=m))
+        _, _, _, k0, k1, _ = pipelined(ctx, 1, kp_steps, bufs, dev_submit)
         ctx.set_timing(False)
         stats, stat_steps = stats_delta(k0, k1), kp_steps
         kernel_timing = (f"per-launch CUDA events in a one-lane pass of {kp_steps} proofs after the timed regions "
                          f"(with {args.plain_lanes} lanes another proof's kernels share the GPU, so a launch's time "
                          "there is not its own)")
+        ctx.set_concurrency(lanes=args.plain_lanes)
     launches_per_proof = sum(s["launches"] for s in stats.values()) / stat_steps
     launches = int(round(launches_per_proof * args.steps))
 
-    # ---- roofline of the dominant kernel
-    peak, peak_kind = peaks()
-    name, s = max(stats.items(), key=lambda kv: kv[1]["ms"])
-    per_launch_bytes = s["bytes"] / max(s["launches"], 1)
-    per_launch_ms = s["ms"] / max(s["launches"], 1)
-    achieved = per_launch_bytes / (per_launch_ms / 1000.0) / 1e9 if per_launch_ms > 0 else 0.0
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        ratio = json.load(open(tfile)).get(name, {}).get("traffic_over_algorithmic")
-        if ratio:
-            traffic = per_launch_bytes * ratio
-    roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": per_launch_bytes, "launches": s["launches"],
-                "ms_per_launch": per_launch_ms}
+    # ---- parity of the timed circuit: the golden of the compiled reference at 8 copies, and
+    # the library's verifier (Verifier::verify) on one timed 1024-copy proof
+    parity = None
+    if not args.no_parity and D.rank == 0:
+        parity = golden_parity(ctx, dc, circ)
+        t0 = time.perf_counter()
+        ok = ctx.verify(dc, bufs[0][0][:plen], bufs[0][1])
+        parity["timed_proof_verified"] = bool(ok)
+        parity["verify_s"] = time.perf_counter() - t0
+
+    # ---- the same proofs with the Keccak-256 transcript (host hashing of the commitment,
+    # challenges and grinding with Keccak-f[1600] instead of SHA-256)
+    keccak = None
+    if not args.no_keccak:
+        ctx.set_fs_hash("Keccak256")
+        nk = min(args.steps, 8)
+        k_ms, _, k_lat, _, _, _ = pipelined(ctx, 2, nk, bufs, dev_submit)
+        ktail = [bytes(b[0][plen - 4096:plen]) for b in bufs[:min(depth, nk + 2)]]
+        ctx.set_fs_hash("SHA256")
+        keccak = {"proofs_per_s": nk / (k_ms / 1000.0), "ms_per_proof": k_ms / nk, "steps": nk,
+                  "consistent": all(t == ktail[0] for t in ktail) and ktail[0] != tail[0],
+                  "note": f"Keccak-256 transcript, {args.plain_lanes} device lanes, {depth} in flight, device input"}
+
+    roofline = roofline_of(stats, traffic)
     total_bytes = sum(v["bytes"] for v in stats.values()) / stat_steps
     kernel_ms = sum(v["ms"] for v in stats.values()) / stat_steps
-    kernels = {k: {"launches_per_step": v["launches"] / stat_steps, "ms_per_step": v["ms"] / stat_steps,
-                   "GBps": (v["bytes"] / (v["ms"] / 1000.0) / 1e9) if v["ms"] else None}
-               for k, v in stats.items() if v["launches"]}
+    kernels = kernel_table(stats, stat_steps, traffic)
+    din.free()
+    ctx.close()
+
+    # ---- batched vs plain on a shortened mixed workload (the metric's own comparison)
+    batched = None
+    if not args.no_batched and D.rank == 0:
+        batched = measure_mixed(device, args.batched_proofs, args.lanes, int(args.budget_gb * (1 << 30)))
 
     cpu = None
     if D.rank == 0 and not args.no_cpu_baseline:
-        vals, info = cpu_sample(circ, args)
+        vals, _, info = cpu_sample(circ, args)
         cpu = dict(info, value=vals[0], unit=UNIT)
 
     if D.rank == 0:
@@ -408,12 +524,13 @@ def run_ours(args, D):
                 "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
                 "config": dict(cfg, parallelism=f"replicas x{D.world}" if D.world > 1 else "single",
                                pipeline=f"{depth} proofs in flight, {args.plain_lanes} device lane(s) (that many "
-                                        "proofs' device stages overlap); timed region = device end of the last "
-                                        "warm-up proof to the last device end among the timed proofs"),
+                                        "proofs' device stages overlap); timed region = earliest device-stage "
+                                        "beginning to latest device-stage end among the timed proofs"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "autotune": tiles,
-                "clocks": clk,
+                "clocks": clk, "parity": parity, "plain_one_lane": plain1, "keccak": keccak, "batched": batched,
                 "latency_ms": {"p50": statistics.median(lat_ms), "p99": float(np.percentile(lat_ms, 99)),
-                               "device_end_intervals_ms": step_ms},
+                               "device_end_intervals_ms": step_ms,
+                               "device_stage_ms_median": statistics.median(stage_ms)},
                 "hbm": {"algorithmic_bytes_per_proof": total_bytes,
                         "GBps_over_step": total_bytes / (max_ms / args.steps / 1000.0) / 1e9,
                         "GBps_over_kernels": total_bytes / (kernel_ms / 1000.0) / 1e9,
@@ -450,20 +567,20 @@ class MixedSet:
             return list(ex.map(lambda i: hashlib.sha256(self.proofs[i].tobytes()).hexdigest(), idx))
 
 
-def run_mixed(args, D):
-    """Plain (one proof at a time) vs continuous batching on the same independent proofs."""
+def measure_mixed(device, n_proofs, lanes, budget, seed=3):
+    """Plain (one proof at a time, one device lane) vs continuous batching (every proof
+    queued at once, up to `lanes` device stages overlapping under the HBM budget) on the
+    same independent mixed proofs; both modes' proofs are compared byte for byte."""
     from gkr_gb300.prover import Context
-    if D.rank != 0:
-        return
-    ctx = Context(D.local_rank)
+    ctx = Context(device)
     t0 = time.perf_counter()
-    ms = MixedSet(ctx, args.proofs)
+    ms = MixedSet(ctx, n_proofs, seed=seed)
     setup_s = time.perf_counter() - t0
     n = len(ms.specs)
     idx = list(range(n))
 
-    # plain: one proof's device stage at a time, each proof submitted after the previous one
-    # finished (the reference's one-proof-per-call usage, on the GPU)
+    # plain: each proof submitted after the previous one finished (the reference's
+    # one-proof-per-call usage, on the GPU)
     ctx.set_concurrency(lanes=1)
     for i in range(min(4, n)):
         ctx.wait(ms.submit(ctx, i))
@@ -476,18 +593,14 @@ def run_mixed(args, D):
     plain_s = time.perf_counter() - t0
     ref = ms.digests(idx)
 
-    # batched: every proof queued at once; up to `lanes` device stages overlap, admitted by
-    # the HBM budget as earlier proofs finish
-    budget = int(args.budget_gb * (1 << 30))
-    ctx.set_concurrency(lanes=args.lanes, hbm_budget_bytes=budget)
-    warm = [ms.submit(ctx, i) for i in range(min(2 * args.lanes, n))]
+    ctx.set_concurrency(lanes=lanes, hbm_budget_bytes=budget)
+    warm = [ms.submit(ctx, i) for i in range(min(2 * lanes, n))]
     for j in warm:
         ctx.wait(j)
-    clocks = ClockSampler(D.local_rank)
+    clocks = ClockSampler(device)
     clocks.start()
     t0 = time.perf_counter()
-    sub = {}
-    jobs = []
+    sub, jobs = {}, []
     for i in idx:
         sub[i] = time.perf_counter()
         jobs.append(ms.submit(ctx, i))
@@ -499,21 +612,34 @@ def run_mixed(args, D):
     clk = clocks.stop()
     same = ms.digests(idx) == ref
     mem = ctx.memory_stats()
-    value = n / batch_s
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": n, "warmup": len(warm),
-            "ms_per_step": batch_s * 1000.0 / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "u32", "data": "synthetic",
-            "config": {"workload": f"{n} independent proofs, depth 4..24, width 2^8..2^18, 16..256 copies, "
-                                   "50% mul uniform wiring, own seed each (one batch)",
-                       "lanes": args.lanes, "hbm_budget_bytes": budget, "setup_s": setup_s,
-                       "witness_bytes_total": ms.bytes,
-                       "timing": "host wall clock from the first submit to the last proof returned"},
-            "batched": {"proofs_per_s": value, "seconds": batch_s,
-                        "latency_ms": {"p50": statistics.median(done), "p99": float(np.percentile(done, 99))}},
-            "plain": {"proofs_per_s": n / plain_s, "seconds": plain_s,
-                      "latency_ms": {"p50": statistics.median(lat_plain), "p99": float(np.percentile(lat_plain, 99))}},
-            "batched_over_plain": (n / batch_s) / (n / plain_s), "byte_identical_to_plain": same,
-            "hbm": {"workspace_peak_bytes": mem["peak"], "budget": mem["budget"]}, "clocks": clk}
+    out = {"workload": f"{n} independent proofs, depth 4..24, width 2^8..2^18, 16..256 copies, 50% mul uniform "
+                       "wiring, own seed each", "proofs": n, "lanes": lanes, "hbm_budget_bytes": budget,
+           "setup_s": setup_s, "witness_bytes_total": ms.bytes,
+           "timing": "host wall clock from the first submit to the last proof returned",
+           "batched": {"proofs_per_s": n / batch_s, "seconds": batch_s,
+                       "latency_ms": {"p50": statistics.median(done), "p99": float(np.percentile(done, 99))}},
+           "plain": {"proofs_per_s": n / plain_s, "seconds": plain_s,
+                     "latency_ms": {"p50": statistics.median(lat_plain), "p99": float(np.percentile(lat_plain, 99))}},
+           "batched_over_plain": plain_s / batch_s, "byte_identical_to_plain": same,
+           "hbm": {"workspace_peak_bytes": mem["peak"], "budget": mem["budget"]}, "clocks": clk}
+    ctx.close()
+    return out
+
+
+def run_mixed(args, D):
+    """Plain (one proof at a time) vs continuous batching on the same independent proofs."""
+    if D.rank != 0:
+        return
+    r = measure_mixed(D.local_rank, args.proofs, args.lanes, int(args.budget_gb * (1 << 30)))
+    n = r["proofs"]
+    line = {"metric": METRIC, "value": r["batched"]["proofs_per_s"], "unit": UNIT, "n_gpus": 1, "steps": n,
+            "warmup": min(2 * args.lanes, n), "ms_per_step": r["batched"]["seconds"] * 1000.0 / n,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": r["workload"] + " (one batch)", "lanes": args.lanes,
+                       "hbm_budget_bytes": r["hbm_budget_bytes"], "setup_s": r["setup_s"],
+                       "witness_bytes_total": r["witness_bytes_total"], "timing": r["timing"]},
+            "batched": r["batched"], "plain": r["plain"], "batched_over_plain": r["batched_over_plain"],
+            "byte_identical_to_plain": r["byte_identical_to_plain"], "hbm": r["hbm"], "clocks": r["clocks"]}
     print(json.dumps(line), flush=True)
 
 
@@ -621,7 +747,7 @@ def run_bn254(args, D):
     ctx.set_timing(one_lane)
     clocks = ClockSampler(D.local_rank)
     clocks.start()
-    total_ms, step_ms, lat_ms, s0, s1 = pipelined(
+    total_ms, step_ms, lat_ms, s0, s1, _ = pipelined(
         ctx, args.warmup, args.steps, bufs, lambda b, m: ctx.submit(dc, None, b[0], b[1], d_input=din.ptr, marker=m))
     clk = clocks.stop()
     ctx.set_timing(False)
@@ -631,8 +757,8 @@ def run_bn254(args, D):
     if not args.no_e2e:
         h0 = ctx.transfer_stats()
         e2e_warm = max(1, args.warmup)
-        e2e_ms, _, e2e_lat, _, _ = pipelined(ctx, e2e_warm, args.steps, bufs,
-                                            lambda b, m: ctx.submit(dc, witness, b[0], b[1], marker=m))
+        e2e_ms, _, e2e_lat, _, _, _ = pipelined(ctx, e2e_warm, args.steps, bufs,
+                                               lambda b, m: ctx.submit(dc, witness, b[0], b[1], marker=m))
         h1 = ctx.transfer_stats()
         n_jobs = e2e_warm + args.steps
         e2e = {"value": args.steps / (e2e_ms / 1000.0), "unit": UNIT,
@@ -642,8 +768,8 @@ def run_bn254(args, D):
     if not one_lane:
         ctx.set_concurrency(lanes=1)
         ctx.set_timing(True)
-        _, _, _, k0, k1 = pipelined(ctx, 1, 2, bufs,
-                                    lambda b, m: ctx.submit(dc, None, b[0], b[1], d_input=din.ptr, marker=m))
+        _, _, _, k0, k1, _ = pipelined(ctx, 1, 2, bufs,
+                                       lambda b, m: ctx.submit(dc, None, b[0], b[1], d_input=din.ptr, marker=m))
         ctx.set_timing(False)
         stats, stat_steps = stats_delta(k0, k1), 2
         kernel_timing = (f"per-launch CUDA events in a one-lane pass of 2 proofs after the timed regions (with "

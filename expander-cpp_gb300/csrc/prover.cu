@@ -387,7 +387,10 @@ struct gkrgpu_ctx {
     // launch accounting: totals read under stats_m; lanes fold each finished job in
     bool timing = false;
     std::atomic<uint64_t> h2d_bytes{0}, d2h_bytes{0};
-    cudaEvent_t markers[64] = {};
+    // timing markers: slots 0..63 hold gkrgpu_mark events and the device-stage ends of
+    // proofs submitted with marker k (slot k); slots 64..127 the device-stage beginnings
+    // of those proofs (slot 64 + k) and further gkrgpu_mark events
+    cudaEvent_t markers[128] = {};
     std::mutex stats_m;
     uint64_t launches[K_NUM_KERNELS] = {};
     double ms[K_NUM_KERNELS] = {};
@@ -1244,6 +1247,13 @@ void gpu_worker(gkrgpu_ctx* c, Lane* lane) {
         const uint64_t need = bn ? workspace_bytes_bn(*j->circuit, j->N, true)
                                  : workspace_bytes(*j->circuit, j->N, j->R, j->d_input == nullptr, true);
         c->acquire_hbm(need);
+        if (j->marker >= 0) {
+            // the device stage begins: this lane's stream has finished its previous proof
+            std::lock_guard<std::mutex> lk(c->stats_m);
+            cudaEvent_t& ev = c->markers[64 + j->marker];
+            if (!ev) cudaEventCreate(&ev);
+            if (ev) cudaEventRecord(ev, lane->stream);
+        }
         try {
             auto wait_host = [&] {
                 std::unique_lock<std::mutex> lk(j->m);
@@ -1739,7 +1749,7 @@ int gkrgpu_reset_stats(gkrgpu_ctx* ctx) {
 int gkrgpu_mark(gkrgpu_ctx* ctx, int slot) {
     return guarded([&] {
         check_ctx(ctx);
-        if (slot < 0 || slot >= 64) fail(GKRGPU_ERR_INVALID, "marker slot must be in [0, 64)");
+        if (slot < 0 || slot >= 128) fail(GKRGPU_ERR_INVALID, "marker slot must be in [0, 128)");
         on_idle_lane(ctx, [&](Lane& c) {
             std::lock_guard<std::mutex> lk(ctx->stats_m);
             if (!ctx->markers[slot]) ck(cudaEventCreate(&ctx->markers[slot]), "cudaEventCreate");
@@ -1754,8 +1764,8 @@ int gkrgpu_elapsed_ms(gkrgpu_ctx* ctx, int from_slot, int to_slot, double* ms) {
         cudaEvent_t a, b;
         {
             std::lock_guard<std::mutex> lk(ctx->stats_m);
-            if (!ms || from_slot < 0 || from_slot >= 64 || to_slot < 0 || to_slot >= 64 || !ctx->markers[from_slot] ||
-                !ctx->markers[to_slot])
+            if (!ms || from_slot < 0 || from_slot >= 128 || to_slot < 0 || to_slot >= 128 ||
+                !ctx->markers[from_slot] || !ctx->markers[to_slot])
                 fail(GKRGPU_ERR_INVALID, "unrecorded marker slot");
             a = ctx->markers[from_slot];
             b = ctx->markers[to_slot];
@@ -1773,6 +1783,42 @@ int gkrgpu_transfer_stats(gkrgpu_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_by
         check_ctx(ctx);
         if (h2d_bytes) *h2d_bytes = ctx->h2d_bytes;
         if (d2h_bytes) *d2h_bytes = ctx->d2h_bytes;
+    });
+}
+
+int gkrgpu_proof_write(const char* path, const uint8_t* proof, uint64_t proof_len) {
+    return guarded([&] {
+        if (!path || (!proof && proof_len)) fail(GKRGPU_ERR_INVALID, "null argument");
+        // the length field is 32 bits (transcript.hpp:56-59 writes bytes.size() as uint32)
+        if (proof_len > 0xffffffffull) fail(GKRGPU_ERR_INVALID, "proof of %llu bytes does not fit the 4-byte length",
+                                            (unsigned long long)proof_len);
+        FILE* f = fopen(path, "wb");
+        if (!f) fail(GKRGPU_ERR_IO, "cannot open %s for writing", path);
+        const uint32_t n = (uint32_t)proof_len;
+        const uint8_t len[4] = {(uint8_t)n, (uint8_t)(n >> 8), (uint8_t)(n >> 16), (uint8_t)(n >> 24)};
+        const bool ok = fwrite(len, 1, 4, f) == 4 && (n == 0 || fwrite(proof, 1, n, f) == n);
+        if (fclose(f) != 0 || !ok) fail(GKRGPU_ERR_IO, "write to %s failed", path);
+    });
+}
+
+int gkrgpu_proof_read(const char* path, uint8_t* buf, uint64_t cap, uint64_t* proof_len) {
+    return guarded([&] {
+        if (!path || !proof_len) fail(GKRGPU_ERR_INVALID, "null argument");
+        FILE* f = fopen(path, "rb");
+        if (!f) fail(GKRGPU_ERR_IO, "cannot open %s", path);
+        struct Closer {
+            FILE* f;
+            ~Closer() { fclose(f); }
+        } closer{f};
+        uint8_t len[4];
+        if (fread(len, 1, 4, f) != 4) fail(GKRGPU_ERR_IO, "%s: no 4-byte length", path);
+        const uint64_t n = (uint64_t)len[0] | ((uint64_t)len[1] << 8) | ((uint64_t)len[2] << 16) | ((uint64_t)len[3] << 24);
+        *proof_len = n;
+        if (!buf) return;  // size query
+        if (cap < n) fail(GKRGPU_ERR_CAPACITY, "proof needs %llu bytes, buffer has %llu", (unsigned long long)n,
+                          (unsigned long long)cap);
+        if (n && fread(buf, 1, n, f) != n) fail(GKRGPU_ERR_IO, "%s: truncated (length field says %llu bytes)", path,
+                                                (unsigned long long)n);
     });
 }
 

@@ -9,7 +9,7 @@ import os
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libgkrgpu.so")
 
-OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_CAPACITY, ERR_TIMEOUT, ERR_STATE = range(7)
+OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_CAPACITY, ERR_TIMEOUT, ERR_STATE, ERR_IO = range(8)
 
 # Field_type numbering of include/configuration/config.hpp:12-16 (GKRGPU_FIELD_*).
 FIELDS = {"M31": 0, "BabyBear": 1, "BN254": 2}
@@ -95,6 +95,8 @@ SIGNATURES = [
     ("gkrgpu_mark", _I, [_P, _I]),
     ("gkrgpu_elapsed_ms", _I, [_P, _I, _I, ctypes.POINTER(ctypes.c_double)]),
     ("gkrgpu_transfer_stats", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
+    ("gkrgpu_proof_write", _I, [ctypes.c_char_p, _P, _U64]),
+    ("gkrgpu_proof_read", _I, [ctypes.c_char_p, _P, _U64, ctypes.POINTER(_U64)]),
 ]
 
 _lib = None

@@ -304,3 +304,8 @@ def config2_circuit(seed=2024, n_layers=24, wide=20, narrow=18):
     local to 2^12-gate windows with probability 0.8."""
     widths = [narrow if l % 2 == 0 else wide for l in range(n_layers + 1)]
     return random_circuit(seed, widths, p_mul=0.6, p_local=0.8, window=1 << 12)
+
+
+def config4_circuit(seed=4254, n_layers=16, width=16):
+    """BN254 plain workload: 16 layers of 2^16 gates, 50% mul / 50% add, uniform wiring."""
+    return uniform_circuit(seed, n_layers, width, p_mul=0.5)

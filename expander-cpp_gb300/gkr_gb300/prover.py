@@ -11,7 +11,7 @@ The circuit input (the reference's layers[0].input_layer_vals) is a (2^n, N) uin
 set with Circuit.set_input or passed to prove() directly.
 """
 import ctypes
-import struct
+import os
 
 import numpy as np
 
@@ -71,15 +71,19 @@ class Proof:
         return isinstance(other, Proof) and self.bytes == other.bytes
 
     def write(self, path):
-        with open(path, "wb") as f:
-            f.write(struct.pack("<I", len(self.bytes) & 0xFFFFFFFF))
-            f.write(self.bytes)
+        """Proof::write_and_compress without the tar step (gkrgpu_proof_write)."""
+        b = np.frombuffer(self.bytes, np.uint8)
+        _lib.check(_lib.load().gkrgpu_proof_write(os.fsencode(path), b.ctypes.data if b.size else None, b.size))
 
     @staticmethod
     def read(path):
-        with open(path, "rb") as f:
-            (n,) = struct.unpack("<I", f.read(4))
-            return Proof(f.read(n))
+        """Proof::read_proof (gkrgpu_proof_read)."""
+        lib = _lib.load()
+        n = ctypes.c_uint64()
+        _lib.check(lib.gkrgpu_proof_read(os.fsencode(path), None, 0, ctypes.byref(n)))
+        buf = np.empty(max(n.value, 1), np.uint8)
+        _lib.check(lib.gkrgpu_proof_read(os.fsencode(path), buf.ctypes.data, buf.nbytes, ctypes.byref(n)))
+        return Proof(buf[:n.value].tobytes())
 
 
 class DeviceCircuit:

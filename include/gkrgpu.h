@@ -32,6 +32,7 @@ extern "C" {
 #define GKRGPU_ERR_CAPACITY 4  /* caller buffer too small (required size still reported) */
 #define GKRGPU_ERR_TIMEOUT 5   /* a bounded wait expired */
 #define GKRGPU_ERR_STATE 6     /* object used in the wrong state */
+#define GKRGPU_ERR_IO 7        /* file could not be opened, read or written */
 
 /* Field_type, include/configuration/config.hpp:12-16 (same numbering).  BabyBear is
  * declared there without a prover and is rejected here too. */
@@ -185,8 +186,9 @@ int gkrgpu_verify(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_cop
  * earlier proofs' device stages run on the GPU, and device stages run one at a time in
  * submission order.  The input (host memory, or device memory with input_on_device = 1),
  * proof_out and claimed_v must stay valid until gkrgpu_prove_wait returns.  With
- * marker_slot >= 0 the device stage's end is recorded as timing marker `marker_slot`
- * (gkrgpu_elapsed_ms).  gkrgpu_prove_wait blocks until the job is finished, frees it and
+ * marker_slot in [0, 64) the device stage's end is recorded as timing marker
+ * `marker_slot` and its beginning (when a lane takes the proof, once that lane's stream has
+ * finished its previous proof) as marker 64 + marker_slot (gkrgpu_elapsed_ms).  gkrgpu_prove_wait blocks until the job is finished, frees it and
  * returns its status; proof_len receives the proof length.  gkrgpu_prove and
  * gkrgpu_prove_device are submit + wait.  No counterpart in the reference (one proof per
  * thread there, bench_keccak.cpp:82-93). */
@@ -234,9 +236,10 @@ int gkrgpu_eval_multilinear(gkrgpu_ctx* ctx, const uint32_t* d_evals, uint32_t n
  * (held by every GPU that loads the library until the process exits), so the limits are
  * nb_vars <= 18, n_copies <= 4096 (a multiple of 4) and n_points <= 3; larger sizes are
  * rejected with GKRGPU_ERR_INVALID.  The first call on a device looks up the scratch
- * address; make that first call before any stream capture.  All calls share the one
- * scratch region: calls that overlap on the GPU (from several host threads or streams)
- * race and must be serialized by the caller. */
+ * address; make that first call before any stream capture begins.  Every call waits for
+ * its own work on `stream` before it returns.  All calls share the one scratch region:
+ * calls that overlap on the GPU (from several host threads or streams) race and must be
+ * serialized by the caller. */
 int gkrgpu_eval_multilinear_noalloc(const uint32_t* d_evals, uint32_t nb_vars, uint32_t n_copies,
                                     const uint32_t* r, int n_points, uint32_t* d_out, void* stream);
 
@@ -277,13 +280,24 @@ typedef struct {
 int gkrgpu_autotune(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
                     const uint32_t* input, int input_on_device, gkrgpu_tile_choice* out, int cap);
 
-/* Timing markers: gkrgpu_mark records CUDA event `slot` (0..63) on the context's stream;
- * gkrgpu_elapsed_ms waits for `to_slot` and returns the device time between the two. */
+/* Timing markers: gkrgpu_mark records CUDA event `slot` (0..127) on the context's stream
+ * once every queued proof has finished; gkrgpu_elapsed_ms waits for `to_slot` and returns
+ * the device time between the two.  Slots 0..63 and 64..127 are also written by proofs
+ * submitted with a marker slot (their device-stage end and beginning). */
 int gkrgpu_mark(gkrgpu_ctx* ctx, int slot);
 int gkrgpu_elapsed_ms(gkrgpu_ctx* ctx, int from_slot, int to_slot, double* ms);
 
 /* Bytes the library copied host->device and device->host since the last reset. */
 int gkrgpu_transfer_stats(gkrgpu_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
+
+/* Proof files in the reference's format, Proof::write_and_compress / read_proof
+ * (include/fiat_shamir/transcript.hpp:54-84): a 4-byte little-endian length, then the proof
+ * bytes.  The reference also tars the file (a shell call); that step is left to the caller.
+ * gkrgpu_proof_write rejects proofs of 2^32 bytes or more (the reference would truncate the
+ * length).  gkrgpu_proof_read with buf = NULL returns the length only; a buffer smaller than
+ * the length gives GKRGPU_ERR_CAPACITY with proof_len set; a short file GKRGPU_ERR_IO. */
+int gkrgpu_proof_write(const char* path, const uint8_t* proof, uint64_t proof_len);
+int gkrgpu_proof_read(const char* path, uint8_t* buf, uint64_t cap, uint64_t* proof_len);
 
 #ifdef __cplusplus
 }

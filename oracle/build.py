@@ -2,7 +2,9 @@
 
 ``build_oracle()`` compiles the C restatement into ``oracle/build/libgkr_oracle.so``
 with plain ``gcc -O3`` (portable: no -march flags, builds on x86-64 and aarch64).
-``build_ref()`` runs ``oracle/build_ref.sh`` when the reference tree exists.
+``build_ref()`` runs ``oracle/build_ref.sh`` when the reference tree exists; its location
+comes from the environment variable GKR_REFERENCE_ROOT (no default: without it the compiled
+reference is simply not built, and the tests that need it skip).
 """
 import os
 import subprocess
@@ -11,7 +13,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "build")
 ORACLE_SO = os.path.join(BUILD, "libgkr_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libgkr_ref.so")
-REFERENCE_ROOT = "/root/reference"
+
+
+def reference_root():
+    """The reference checkout named by GKR_REFERENCE_ROOT, or None."""
+    root = os.environ.get("GKR_REFERENCE_ROOT", "")
+    return root if root and os.path.isdir(os.path.join(root, "include", "LinearGKR")) else None
 
 
 def _stale(target, sources):
@@ -36,14 +43,15 @@ def build_oracle(force=False):
 
 def build_ref(force=False):
     """Compile the reference driver (x86-64 only, needs the reference tree)."""
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "include", "LinearGKR")):
-        return None
+    root = reference_root()
+    if root is None:
+        return REF_SO if os.path.exists(REF_SO) and os.uname().machine == "x86_64" else None
     if os.uname().machine != "x86_64":
         return None
     srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "build_ref.sh"), os.path.join(HERE, "bn254.h")]
     if not force and not _stale(REF_SO, srcs):
         return REF_SO
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT])
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), root])
     return REF_SO
 
 

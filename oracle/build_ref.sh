@@ -4,9 +4,10 @@
 # Test infrastructure only; x86-64 with AVX-512 (the reference's own flags,
 # CMakeLists.txt:9-12).  -DDISABLE_OPTIMIZED_SHA256 keeps the generic SHA-256 transform,
 # which is the one the reference uses (its SSE4/AVX2/SHA-NI sources are not vendored).
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT   (or GKR_REFERENCE_ROOT in the environment)
 set -e
-REF=${1:-/root/reference}
+REF=${1:-$GKR_REFERENCE_ROOT}
+[ -n "$REF" ] || { echo "usage: $0 REFERENCE_ROOT (or set GKR_REFERENCE_ROOT)" >&2; exit 2; }
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 [ -d "$REF/include/LinearGKR" ] || { echo "reference tree not found at $REF" >&2; exit 3; }

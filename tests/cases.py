@@ -66,10 +66,23 @@ CASES = {
 }
 
 
+# The benchmark's own circuits at copy counts the reference proves in seconds: the config-2
+# proof (24 layers alternating 2^18 / 2^20 gates, 60% mul, window-local wiring) and, below,
+# the config-4 BN254 proof (16 layers of 2^16 gates).  Their witness seeds are recorded in
+# the golden file, so the benchmark can rebuild the same inputs without this module.
+LARGE_CASES = {
+    "cfg2_n8": lambda: (gc.config2_circuit(), 8, 10),
+    "cfg2_n16": lambda: (gc.config2_circuit(), 16, 10),
+}
+
+
+def witness_seed(name):
+    return sum(ord(c) for c in name) * 7919
+
+
 def build(name):
-    circ, n, grind = CASES[name]()
-    seed = sum(ord(c) for c in name) * 7919
-    return circ, gc.random_witness(seed, circ.log_input_size, n), grind
+    circ, n, grind = {**CASES, **LARGE_CASES}[name]()
+    return circ, gc.random_witness(witness_seed(name), circ.log_input_size, n), grind
 
 
 # ---------------------------------------------------------------- BN254 (Config::field_type = BN254)
@@ -99,11 +112,16 @@ BN_CASES = {
 }
 
 
+BN_LARGE_CASES = {
+    "bn_cfg4_n4": lambda: (gc.config4_circuit(), 4, 10),
+    "bn_cfg4_n8": lambda: (gc.config4_circuit(), 8, 10),
+}
+
+
 def build_bn(name):
     """(circuit, (rows, N, 4) uint64 witness, grinding_bits) of a BN254 case."""
-    circ, n, grind = BN_CASES[name]()
-    seed = sum(ord(c) for c in name) * 7919
-    w = gc.random_witness_bn254(seed, circ.log_input_size, n)
+    circ, n, grind = {**BN_CASES, **BN_LARGE_CASES}[name]()
+    w = gc.random_witness_bn254(witness_seed(name), circ.log_input_size, n)
     if name == "bn_edge_values_n8":
         r_minus_1 = [(gc.BN254_R - 1) >> (64 * k) & (2**64 - 1) for k in range(4)]
         w[0, :, :] = np.array(r_minus_1, np.uint64)  # r - 1 everywhere in row 0

@@ -1,17 +1,19 @@
 """The C++ drop-in adapter (include/gkrgpu.hpp) compiles against the reference's own headers
 and links against libgkrgpu.so: the reference's GKR_WITH_PC_TEST body builds with only the
-prover type swapped.  Needs the reference tree (present where the oracle was built)."""
+prover type swapped.  Needs the reference tree, named by the environment variable
+GKR_REFERENCE_ROOT (x86-64: the reference's SIMD build needs AVX-512)."""
 import os
 import subprocess
 
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+REF = os.environ.get("GKR_REFERENCE_ROOT", "")
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include", "LinearGKR")) or os.uname().machine != "x86_64",
-                    reason="reference tree (x86-64 SIMD build) not available")
+@pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "include", "LinearGKR"))
+                    or os.uname().machine != "x86_64",
+                    reason="reference tree (GKR_REFERENCE_ROOT, x86-64 SIMD build) not available")
 def test_adapter_builds_against_reference(tmp_path):
     from gkr_gb300 import build
     lib = build.build()

@@ -1,20 +1,29 @@
-"""Host logic of bench.py's pipelined timing (no GPU): with several device lanes proofs can
-finish out of order, and the timed region must still end only when every timed proof has
-finished; at most `depth` proofs are in flight, and the kernel statistics bracket the
-timed proofs."""
+"""Host logic of bench.py's pipelined timing (no GPU): the timed region runs from the
+earliest device-stage beginning among the timed proofs to the latest device-stage end among
+them, so a proof whose device work mostly lay before the region cannot be counted inside it;
+with several device lanes proofs can finish out of order; at most `depth` proofs are in
+flight, and the kernel statistics bracket the timed proofs."""
+import pytest
+
 import bench
 
 
 class FakeCtx:
-    """Proof i ends at `ends[i]` ms; a marker records the end of the proof submitted with it."""
+    """Proof i's device stage runs from begins[i] to ends[i] ms after the reference mark.
+    A proof submitted with marker k records its end in slot k and its beginning in slot
+    64 + k; gkrgpu_mark records the reference slot at time 0."""
 
-    def __init__(self, ends):
-        self.ends = ends
+    def __init__(self, begins, ends):
+        self.begins, self.ends = begins, ends
         self.marker_ms = {}
         self.waited = []
         self.in_flight = 0
         self.max_in_flight = 0
         self.next_id = 0
+
+    def mark(self, slot):
+        assert self.in_flight == 0, "the reference mark is taken before any proof is submitted"
+        self.marker_ms[slot] = 0.0
 
     def submit(self, buf, marker):
         i = self.next_id
@@ -23,6 +32,7 @@ class FakeCtx:
         self.max_in_flight = max(self.max_in_flight, self.in_flight)
         if marker >= 0:
             self.marker_ms[marker] = self.ends[i]
+            self.marker_ms[64 + marker] = self.begins[i]
         return i
 
     def wait(self, job):
@@ -36,29 +46,40 @@ class FakeCtx:
         return self.marker_ms[b] - self.marker_ms[a]
 
 
-def run(ends, n_warm, n_timed, depth):
-    ctx = FakeCtx(ends)
+def run(begins, ends, n_warm, n_timed, depth):
+    ctx = FakeCtx(begins, ends)
     bufs = [None] * depth
     out = bench.pipelined(ctx, n_warm, n_timed, bufs, lambda b, m: ctx.submit(b, m))
     return ctx, out
 
 
-def test_region_ends_at_the_last_timed_proof_even_out_of_order():
-    # two lanes: proof 4 (timed) finishes after proof 5 (the last submitted)
-    ends = [10.0, 11.0, 20.0, 21.0, 32.0, 30.0]
-    ctx, (total, steps, lat, s0, s1) = run(ends, n_warm=3, n_timed=3, depth=4)
-    # from the last warm-up proof's end (proof 2) to the latest timed end (proof 4), not to
-    # the end of the last submitted proof (proof 5, 30 ms)
-    assert total == 32.0 - 20.0
-    assert len(steps) == 3 and len(lat) == 3
+def test_region_starts_at_the_first_timed_device_stage_and_ends_at_the_last_end():
+    # two lanes: warm-up proofs 0-2, timed 3-5; proof 3 began at 9.5 (while warm-up proof 2
+    # was still running) and ended at 20.5, just after proof 2; proof 4 (timed) ends after
+    # proof 5, the last one submitted
+    begins = [0.0, 0.0, 10.0, 9.5, 20.5, 21.0]
+    ends = [10.0, 9.5, 20.0, 20.5, 32.0, 30.0]
+    ctx, (total, steps, lat, s0, s1, stage) = run(begins, ends, n_warm=3, n_timed=3, depth=4)
+    # from proof 3's beginning, not from the end of the last warm-up proof (20.0), which would
+    # count proof 3's 11 ms of device work inside a 12 ms window
+    assert total == 32.0 - 9.5
+    assert steps == [20.5 - 9.5, 30.0 - 20.5, 32.0 - 30.0]
+    assert stage == [11.0, 11.5, 9.0]
+    assert len(lat) == 3
     assert ctx.max_in_flight <= 4
     assert s0["k"]["launches"] == 3 and s1["k"]["launches"] == 6
 
 
 def test_in_order_region_and_depth_bound():
-    ends = [float(10 * i) for i in range(8)]
-    ctx, (total, steps, _, _, _) = run(ends, n_warm=3, n_timed=5, depth=2)
-    assert total == 70.0 - 20.0
+    ends = [float(10 * (i + 1)) for i in range(8)]
+    begins = [e - 10.0 for e in ends]
+    ctx, (total, steps, _, _, _, _) = run(begins, ends, n_warm=3, n_timed=5, depth=2)
+    assert total == 80.0 - 30.0
     assert steps == [10.0] * 5
     assert ctx.max_in_flight <= 2
     assert ctx.waited == list(range(8))
+
+
+def test_timed_proofs_fit_the_marker_slots():
+    with pytest.raises(ValueError):
+        bench.pipelined(FakeCtx([0.0] * 70, [1.0] * 70), 1, bench.MAX_TIMED + 1, [None], lambda b, m: 0)

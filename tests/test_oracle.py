@@ -16,7 +16,9 @@ import pytest
 import cases
 from gkr_gb300 import circuit as gc
 
-GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))["cases"]
+_ALL = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
+GOLDEN = _ALL["cases"]
+LARGE = _ALL.get("large_cases", {})
 
 
 def sha(b):
@@ -41,6 +43,18 @@ def test_oracle_reproduces_reference_golden(oracle, name):
     assert sha(ev[-1].tobytes()) == g["output_sha256"]
     assert sha(np.concatenate(ev).tobytes()) == g["values_sha256"]
     assert oracle.verify(circ, w, cv, proof, grinding_bits=grind)
+
+
+def test_oracle_reproduces_reference_golden_config2(oracle):
+    """The benchmark's config-2 circuit (24 layers alternating 2^18 / 2^20 gates) at 8
+    copies: the restatement reproduces the compiled reference's proof byte for byte."""
+    name = "cfg2_n8"
+    g = LARGE[name]
+    circ, w, grind = cases.build(name)
+    cv, proof = oracle.prove(circ, w, grinding_bits=grind)
+    assert len(proof) == g["proof_len"]
+    assert sha(proof) == g["proof_sha256"]
+    assert sha(cv.tobytes()) == g["claimed_v_sha256"]
 
 
 def test_oracle_rejects_tampering(oracle):
