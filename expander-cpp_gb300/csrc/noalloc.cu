@@ -27,7 +27,11 @@ constexpr uint32_t kMaxCopies = 4096;   // up to 4096 copies per row
 constexpr int kMaxPoints = 3;           // up to 3 evaluation points per call
 constexpr size_t kEqBytes = (size_t)kMaxPoints * (1u << kMaxVars) * 4;  // 3 MiB of eq tables
 constexpr size_t kAccBytes = (size_t)kMaxPoints * kMaxCopies * 8;       // 96 KiB of 64-bit sums
-constexpr size_t kTicketBytes = 256;
+// One arrival ticket per lane group of the reduction: a group covers 4 * tpr copies, so
+// 4096 copies at one thread per row slice (tpr = 1, when n_copies / 4 has no larger
+// divisor up to 32) give the most groups, 1024.
+constexpr uint32_t kMaxLaneGroups = kMaxCopies / 4;
+constexpr size_t kTicketBytes = (size_t)kMaxLaneGroups * 4;
 constexpr size_t kScratchBytes = kEqBytes + kAccBytes + kTicketBytes;
 
 // The scratch.  Host code must not use this name as an address (it is a host-side stand-in
@@ -112,6 +116,8 @@ extern "C" int gkrgpu_eval_multilinear_noalloc(const uint32_t* d_evals, uint32_t
     g.tpr = Q <= 32 ? Q : 32;
     while (Q % g.tpr) g.tpr--;
     g.rps = 256 / g.tpr;
+    if (Q % g.tpr || Q / g.tpr > kMaxLaneGroups)
+        return fail(GKRGPU_ERR_INVALID, "no row tile with at most 1024 lane groups for this copy count");
     e = gkrgpu::launch_wsum(n_points, d_evals, 1ull << nb_vars, eq, g, 256, (uint32_t)g_sm_count[dev] * 4, red, d_out, s);
     if (e != cudaSuccess) return fail(GKRGPU_ERR_CUDA, cudaGetErrorString(e));
     e = cudaStreamSynchronize(s);

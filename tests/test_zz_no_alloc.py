@@ -18,7 +18,11 @@ from gkr_gb300 import circuit as gc
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("nb_vars,n,points", [(18, 64, 3), (12, 4096, 2), (6, 4, 1), (0, 8, 3)])
+# 1028, 2044 and 4084 copies: n_copies / 4 has no divisor between 2 and 32 (257 is prime,
+# 511 = 7 x 73, 1021 is prime, so row slices of 4 or 28 copies), giving 257, 73 and 1021
+# lane groups, each with its own arrival ticket in the fixed scratch.
+@pytest.mark.parametrize("nb_vars,n,points", [(18, 64, 3), (12, 4096, 2), (6, 4, 1), (0, 8, 3),
+                                              (10, 1028, 3), (9, 2044, 2), (8, 4084, 1)])
 def test_noalloc_matches_allocating_entry_point(ctx, nb_vars, n, points):
     from gkr_gb300 import _lib
     from gkr_gb300.prover import DeviceBuffer
