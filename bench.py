@@ -79,6 +79,12 @@ def parse():
     ap.add_argument("--no-parity", action="store_true", help="plain: skip the golden and verifier checks")
     ap.add_argument("--rates", default="200,500,1000,2000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=4.0, help="serve: seconds of arrivals per rate")
+    ap.add_argument("--serve-size", choices=["mixed", "config2"], default="mixed",
+                    help="serve: request sizes (the mixed proofs, or the large config-2 proof)")
+    ap.add_argument("--max-queue", type=int, default=512,
+                    help="serve: requests waiting for admission beyond which new ones are rejected")
+    ap.add_argument("--host-threads", type=int, default=0,
+                    help="host threads for the commitment hashes (0: the library default)")
     return ap.parse_args()
 
 
@@ -388,6 +394,8 @@ def run_ours(args, D):
     circ, widths, cfg = workload(args)
     N = args.copies
     ctx = Context(device)
+    if args.host_threads:
+        ctx.set_host_threads(args.host_threads)
     if args.plain_lanes > 1:
         ctx.set_concurrency(lanes=args.plain_lanes)
     if args.tile:
@@ -511,7 +519,8 @@ def run_ours(args, D):
     # ---- batched vs plain on a shortened mixed workload (the metric's own comparison)
     batched = None
     if not args.no_batched and D.rank == 0:
-        batched = measure_mixed(device, args.batched_proofs, args.lanes, int(args.budget_gb * (1 << 30)))
+        batched = measure_mixed(device, args.batched_proofs, args.lanes, int(args.budget_gb * (1 << 30)),
+                                host_threads=args.host_threads)
 
     cpu = None
     if D.rank == 0 and not args.no_cpu_baseline:
@@ -567,12 +576,14 @@ class MixedSet:
             return list(ex.map(lambda i: hashlib.sha256(self.proofs[i].tobytes()).hexdigest(), idx))
 
 
-def measure_mixed(device, n_proofs, lanes, budget, seed=3):
+def measure_mixed(device, n_proofs, lanes, budget, seed=3, host_threads=0):
     """Plain (one proof at a time, one device lane) vs continuous batching (every proof
     queued at once, up to `lanes` device stages overlapping under the HBM budget) on the
     same independent mixed proofs; both modes' proofs are compared byte for byte."""
     from gkr_gb300.prover import Context
     ctx = Context(device)
+    if host_threads:
+        ctx.set_host_threads(host_threads)
     t0 = time.perf_counter()
     ms = MixedSet(ctx, n_proofs, seed=seed)
     setup_s = time.perf_counter() - t0
@@ -621,6 +632,7 @@ def measure_mixed(device, n_proofs, lanes, budget, seed=3):
            "plain": {"proofs_per_s": n / plain_s, "seconds": plain_s,
                      "latency_ms": {"p50": statistics.median(lat_plain), "p99": float(np.percentile(lat_plain, 99))}},
            "batched_over_plain": plain_s / batch_s, "byte_identical_to_plain": same,
+           "host_threads": host_threads or "default",
            "hbm": {"workspace_peak_bytes": mem["peak"], "budget": mem["budget"]}, "clocks": clk}
     ctx.close()
     return out
@@ -630,7 +642,8 @@ def run_mixed(args, D):
     """Plain (one proof at a time) vs continuous batching on the same independent proofs."""
     if D.rank != 0:
         return
-    r = measure_mixed(D.local_rank, args.proofs, args.lanes, int(args.budget_gb * (1 << 30)))
+    r = measure_mixed(D.local_rank, args.proofs, args.lanes, int(args.budget_gb * (1 << 30)),
+                      host_threads=args.host_threads)
     n = r["proofs"]
     line = {"metric": METRIC, "value": r["batched"]["proofs_per_s"], "unit": UNIT, "n_gpus": 1, "steps": n,
             "warmup": min(2 * args.lanes, n), "ms_per_step": r["batched"]["seconds"] * 1000.0 / n,
@@ -643,68 +656,91 @@ def run_mixed(args, D):
     print(json.dumps(line), flush=True)
 
 
-def run_serve(args, D):
-    """Open-loop Poisson arrivals of mixed proofs: continuous batching vs one at a time."""
-    import threading as th
+def serve_rate(srv, dcs, wits, rate, duration, seed):
+    """One open-loop Poisson stream through the server: request r proves proof (r mod n);
+    returns offered / admitted / rejected counts, completed proofs/s and p50 / p99 latency
+    of the completed requests (arrival to proof returned)."""
+    from gkr_gb300.serving import Rejected
+    n = len(dcs)
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * duration * 1.5) + 8))
+    arrivals = arrivals[arrivals < duration]
+    futs = []
+    t0 = time.perf_counter()
+    for r, a in enumerate(arrivals):
+        now = time.perf_counter() - t0
+        if a > now:
+            time.sleep(a - now)
+        futs.append(srv.submit(dcs[r % n], wits[r % n]))
+    lats, rejected = [], 0
+    t_last = t0
+    for f in futs:
+        try:
+            res = f.result()
+            lats.append(res.latency_ms)
+            t_last = max(t_last, time.perf_counter())
+        except Rejected:
+            rejected += 1
+    wall = t_last - t0
+    return {"offered": len(arrivals), "offered_per_s": len(arrivals) / duration, "admitted": len(lats),
+            "rejected": rejected, "completed_per_s": len(lats) / wall if wall > 0 else None,
+            "latency_ms": {"p50": statistics.median(lats), "p99": float(np.percentile(lats, 99))} if lats else None}
 
+
+def run_serve(args, D):
+    """Open-loop Poisson arrivals through the serving loop (gkr_gb300.serving.ProofServer):
+    continuous batching over several device lanes vs one proof at a time (one lane), at each
+    rate.  --serve-size mixed: the mixed proofs (depth 4..24, width 2^8..2^18, 16..256
+    copies); config2: the large proof (two distinct 1 GiB witnesses; one proof's workspace
+    fills most of the budget, so the server runs saturated and its bounded admission queue
+    rejects the rest).  Witnesses are uploaded once per request at admission and stay
+    resident until the proof is done; the proof reads the resident copy."""
+    from gkr_gb300 import circuit as gc
     from gkr_gb300.prover import Context
+    from gkr_gb300.serving import ProofServer
     if D.rank != 0:
         return
     ctx = Context(D.local_rank)
-    ms = MixedSet(ctx, args.proofs, seed=5)
-    n = len(ms.specs)
+    if args.host_threads:
+        ctx.set_host_threads(args.host_threads)
     budget = int(args.budget_gb * (1 << 30))
+    if args.serve_size == "config2":
+        circ = gc.config2_circuit()
+        dc = ctx.load(circ)
+        wits = [gc.random_witness(2000 + i, circ.log_input_size, 1024) for i in range(2)]
+        dcs = [dc] * len(wits)
+        desc = ("open-loop Poisson arrivals of the config-2 proof (24 layers 2^18/2^20, 1024 copies, "
+                "2 distinct witnesses)")
+        arena, max_queue, lanes = 4 << 30, 4, args.plain_lanes
+    else:
+        ms = MixedSet(ctx, args.proofs, seed=5)
+        dcs, wits = ms.dcs, ms.witness
+        desc = (f"open-loop Poisson arrivals over {len(dcs)} distinct mixed proofs (depth 4..24, width 2^8..2^18, "
+                "16..256 copies)")
+        arena, max_queue, lanes = 16 << 30, args.max_queue, args.lanes
     out = {}
-    for mode, lanes in (("batched", args.lanes), ("plain", 1)):
-        ctx.set_concurrency(lanes=lanes, hbm_budget_bytes=budget)
-        for i in range(min(lanes, n)):
-            ctx.wait(ms.submit(ctx, i))
+    clocks = ClockSampler(D.local_rank)
+    clocks.start()
+    for mode, nl in (("batched", lanes), ("plain", 1)):
+        srv = ProofServer(ctx, lanes=nl, budget_bytes=budget, arena_bytes=arena, max_queue=max_queue)
+        for i in range(min(2 * nl, len(dcs))):  # warm-up
+            srv.submit(dcs[i], wits[i]).result()
         res = {}
         for rate in [float(r) for r in args.rates.split(",")]:
-            rng = np.random.default_rng(int(rate))
-            arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * args.duration) + 1))
-            arrivals = arrivals[arrivals < args.duration][: 2 * n]  # bounded so the slow mode drains
-            # each request proves proof (k mod n); a proof's buffers are reused only after its
-            # previous request finished
-            busy = [th.Lock() for _ in range(n)]
-            lats, lock = [], th.Lock()
-            pending = []
-
-            def waiter(job, t_arr, k):
-                ctx.wait(job)
-                t = time.perf_counter()
-                busy[k].release()
-                with lock:
-                    lats.append((t - t_arr) * 1000.0)
-
-            t0 = time.perf_counter()
-            for r, a in enumerate(arrivals):
-                now = time.perf_counter() - t0
-                if a > now:
-                    time.sleep(a - now)
-                k = r % n
-                busy[k].acquire()
-                t_arr = t0 + a
-                job = ms.submit(ctx, k)
-                w = th.Thread(target=waiter, args=(job, t_arr, k))
-                w.start()
-                pending.append(w)
-            for w in pending:
-                w.join()
-            wall = time.perf_counter() - t0
-            window = float(arrivals[-1]) if len(arrivals) > 1 else args.duration
-            res[str(int(rate))] = {"offered": len(arrivals), "offered_per_s": len(arrivals) / window,
-                                   "completed_per_s": len(lats) / wall,
-                                   "latency_ms": {"p50": statistics.median(lats), "p99": float(np.percentile(lats, 99))}}
-        out[mode] = res
+            res[str(int(rate))] = serve_rate(srv, dcs, wits, rate, args.duration, int(rate))
+        res["server"] = srv.stats()
+        srv.close()
+        out[mode] = dict(res, lanes=nl)
+    clk = clocks.stop()
     top = out["batched"][str(int(float(args.rates.split(",")[-1])))]
     line = {"metric": METRIC, "value": top["completed_per_s"], "unit": UNIT, "n_gpus": 1,
-            "steps": top["offered"], "warmup": args.lanes, "ms_per_step": 1000.0 / top["completed_per_s"],
+            "steps": top["admitted"], "warmup": 2 * out["batched"]["lanes"],
+            "ms_per_step": 1000.0 / top["completed_per_s"] if top["completed_per_s"] else None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": f"open-loop Poisson arrivals over {n} distinct mixed proofs (depth 4..24, width "
-                                   "2^8..2^18, 16..256 copies)", "rates": args.rates, "duration_s": args.duration,
-                       "lanes": args.lanes, "hbm_budget_bytes": budget},
-            "serving": out}
+            "config": {"workload": desc, "rates": args.rates, "duration_s": args.duration, "hbm_budget_bytes": budget,
+                       "arena_bytes": arena, "max_queue": max_queue,
+                       "timing": "host wall clock; latency = arrival to proof returned"},
+            "serving": out, "clocks": clk}
     print(json.dumps(line), flush=True)
 
 

@@ -126,7 +126,7 @@ struct BnProver {
     void load_input(const uint32_t* h_input, const uint32_t* d_input) {
         const uint64_t n = C.in_rows(0) * N;
         const uint32_t* src = d_input;
-        if (h_input) {
+        if (h_input && !d_input) {
             c.copy(ws.stage, h_input, n * 32, cudaMemcpyHostToDevice, "input upload");
             src = ws.stage;
         }

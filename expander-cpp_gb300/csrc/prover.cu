@@ -230,6 +230,7 @@ struct Lane {
         size_t e0, e1;
         double bytes;
         uint32_t tag;
+        double host_ms;  // host clock at the launch call, ms after the context's epoch
     };
     // (layer << 16) | (phase << 8) | round of the launches that follow, for the trace
     uint32_t tag = 0;
@@ -352,11 +353,15 @@ struct gkrgpu_ctx {
     std::deque<gkrgpu_job*> host_q, gpu_q;
     std::vector<std::thread> workers;
     std::vector<std::unique_ptr<Lane>> lanes;
-    // host stages (commitment hash, grinding) run on host_workers threads: the SHA-256 of a
+    // host stages (commitment hash, grinding) run on host_workers threads (host_threads_set:
+    // the caller's count, else max(4, min(lanes, 8))): the SHA-256 of a
     // large commitment is sequential, so several proofs' hashes overlap each other
-    int n_lanes = 1, host_workers = 4, running = 0;
+    int n_lanes = 1, host_workers = 4, running = 0, host_threads_set = 0;
     int fs_hash = kFsSha256;  // transcript hash of jobs submitted from now on
     bool stopping = false;
+    // copies of gkrgpu_upload: their own stream, so queued and running proofs go on
+    std::mutex xfer_m;
+    cudaStream_t xfer = nullptr;
 
     void start_workers();
     void shutdown() {
@@ -395,16 +400,26 @@ struct gkrgpu_ctx {
     uint64_t launches[K_NUM_KERNELS] = {};
     double ms[K_NUM_KERNELS] = {};
     double bytes[K_NUM_KERNELS] = {};
-    // per-launch CSV (kernel, layer, phase, round, algorithmic bytes, ms) of timed jobs,
-    // appended to the file named by the environment variable GKRGPU_TRACE
+    // per-launch CSV (kernel, lane, layer, phase, round, algorithmic bytes, ms, device start
+    // and host launch time in ms after the epoch) of timed jobs, appended to the file named by
+    // the environment variable GKRGPU_TRACE
     FILE* trace = nullptr;
+    cudaEvent_t epoch = nullptr;  // recorded at creation when tracing: the trace's time zero
+    std::chrono::steady_clock::time_point epoch_host;
+    int lane_index(const Lane* l) const {
+        for (size_t k = 0; k < lanes.size(); k++)
+            if (lanes[k].get() == l) return (int)k;
+        return -1;
+    }
 
     ~gkrgpu_ctx() {
         DeviceGuard g(device);
         lanes.clear();
         if (trace) fclose(trace);
+        if (epoch) cudaEventDestroy(epoch);
         for (auto e : markers)
             if (e) cudaEventDestroy(e);
+        if (xfer) cudaStreamDestroy(xfer);
         if (pool) cudaMemPoolDestroy(pool);
     }
 
@@ -457,7 +472,9 @@ void Lane::launch(int kid, double algo_bytes, F&& f) {
     if (X->timing) {
         const size_t e1 = next_event();
         ck(cudaEventRecord(events[e1], stream), "cudaEventRecord");
-        recs.push_back({kid, e0, e1, algo_bytes, tag});
+        const double host_ms =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - X->epoch_host).count();
+        recs.push_back({kid, e0, e1, algo_bytes, tag, host_ms});
     }
 }
 
@@ -471,12 +488,18 @@ void Lane::resolve_events() {
         ck(cudaEventElapsedTime(&each[i], events[r.e0], events[r.e1]), "cudaEventElapsedTime");
         t_ms[r.kid] += each[i];
     }
+    std::vector<float> start(X->trace && X->epoch ? recs.size() : 0);
+    for (size_t i = 0; i < start.size(); i++)
+        ck(cudaEventElapsedTime(&start[i], X->epoch, events[recs[i].e0]), "cudaEventElapsedTime");
     std::lock_guard<std::mutex> lk(X->stats_m);
-    if (X->trace)
+    if (X->trace) {
+        const int li = X->lane_index(this);
         for (size_t i = 0; i < recs.size(); i++)
-            fprintf(X->trace, "%s,%u,%u,%u,%.0f,%.6f\n", kKernelNames[recs[i].kid], recs[i].tag >> 16,
-                    (recs[i].tag >> 8) & 0xff, recs[i].tag & 0xff, recs[i].bytes, (double)each[i]);
-    if (X->trace) fflush(X->trace);
+            fprintf(X->trace, "%s,%d,%u,%u,%u,%.0f,%.6f,%.4f,%.4f\n", kKernelNames[recs[i].kid], li, recs[i].tag >> 16,
+                    (recs[i].tag >> 8) & 0xff, recs[i].tag & 0xff, recs[i].bytes, (double)each[i],
+                    start.empty() ? -1.0 : (double)start[i], recs[i].host_ms);
+        fflush(X->trace);
+    }
     recs.clear();
     ev_used = 0;
     for (int k = 0; k < K_NUM_KERNELS; k++) {
@@ -1045,7 +1068,7 @@ struct Prover {
         const uint64_t in_bytes = C.in_rows(0) * (uint64_t)N * 4;
         reserve(d_input == nullptr, true);
         layout_values(d_input);
-        if (h_input) c.copy(vals[0], h_input, in_bytes, cudaMemcpyHostToDevice, "input upload");
+        if (h_input && !d_input) c.copy(vals[0], h_input, in_bytes, cudaMemcpyHostToDevice, "input upload");
         check_input();
         evaluate();
     }
@@ -1260,15 +1283,25 @@ void gpu_worker(gkrgpu_ctx* c, Lane* lane) {
                 j->cv.wait(lk, [&] { return j->host_done; });
                 if (j->host_rc) throw Error(j->host_rc, j->host_err);
             };
+            auto wait_host_traced = [&] {
+                if (!c->trace) return wait_host();
+                const auto t0 = std::chrono::steady_clock::now();
+                wait_host();
+                const auto t1 = std::chrono::steady_clock::now();
+                std::lock_guard<std::mutex> lk(c->stats_m);
+                fprintf(c->trace, "host_stage_wait,%d,0,0,0,0,%.6f,-1,%.4f\n", c->lane_index(lane),
+                        std::chrono::duration<double, std::milli>(t1 - t0).count(),
+                        std::chrono::duration<double, std::milli>(t0 - c->epoch_host).count());
+            };
             if (bn) {
                 BnProver p(*c, *lane, *j->circuit, j->N);
                 p.device_front(j->h_input, j->d_input);
-                wait_host();
+                wait_host_traced();
                 p.device_back(j->ts, j->proof_out, j->claimed_v);
             } else {
                 Prover p(*c, *lane, *j->circuit, j->N, j->R);
                 p.device_front(j->h_input, j->d_input);
-                wait_host();
+                wait_host_traced();
                 p.device_back(j->ts, j->proof_out, j->claimed_v);
             }
             if (j->marker >= 0) {
@@ -1433,6 +1466,12 @@ int gkrgpu_create(int device, gkrgpu_ctx** out) {
         if (const char* tp = getenv("GKRGPU_TRACE"))
             if (*tp) c->trace = fopen(tp, "a");
         c->lane(0);
+        if (c->trace) {
+            ck(cudaEventCreate(&c->epoch), "cudaEventCreate");
+            ck(cudaEventRecord(c->epoch, c->lane(0).stream), "cudaEventRecord");
+            ck(cudaEventSynchronize(c->epoch), "cudaEventSynchronize");
+            c->epoch_host = std::chrono::steady_clock::now();
+        }
         *out = c.release();
     });
 }
@@ -1456,7 +1495,7 @@ int gkrgpu_set_concurrency(gkrgpu_ctx* ctx, int lanes, uint64_t hbm_budget_bytes
         DeviceGuard dg(ctx->device);
         if (lanes) {
             ctx->n_lanes = lanes;
-            ctx->host_workers = std::max(4, std::min(lanes, 8));
+            ctx->host_workers = ctx->host_threads_set ? ctx->host_threads_set : std::max(4, std::min(lanes, 8));
         }
         if (hbm_budget_bytes) {
             ctx->hbm_budget = hbm_budget_bytes;
@@ -1467,6 +1506,19 @@ int gkrgpu_set_concurrency(gkrgpu_ctx* ctx, int lanes, uint64_t hbm_budget_bytes
             std::lock_guard<std::mutex> lk(ctx->qm);
             ctx->stopping = false;
         }
+    });
+}
+
+int gkrgpu_set_host_threads(gkrgpu_ctx* ctx, int threads) {
+    return guarded([&] {
+        check_ctx(ctx);
+        if (threads < 0 || threads > 64) fail(GKRGPU_ERR_INVALID, "threads must be in [1, 64] (0: the default)");
+        ctx->drain();
+        ctx->shutdown();
+        ctx->host_threads_set = threads;
+        ctx->host_workers = threads ? threads : std::max(4, std::min(ctx->n_lanes, 8));
+        std::lock_guard<std::mutex> lk(ctx->qm);
+        ctx->stopping = false;
     });
 }
 
@@ -1562,6 +1614,19 @@ int gkrgpu_prove_submit(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
         *job = nullptr;
         *job = submit(ctx, circuit, n_copies, grinding_bits, input_on_device ? nullptr : input,
                       input_on_device ? input : nullptr, proof_out, proof_cap, claimed_v, marker_slot, nullptr);
+    });
+}
+
+int gkrgpu_prove_submit_resident(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies,
+                                 int grinding_bits, const uint32_t* h_input, const uint32_t* d_input,
+                                 uint8_t* proof_out, uint64_t proof_cap, uint32_t* claimed_v, int marker_slot,
+                                 gkrgpu_job** job) {
+    return guarded([&] {
+        if (!job) fail(GKRGPU_ERR_INVALID, "null job output");
+        *job = nullptr;
+        if (!h_input || !d_input) fail(GKRGPU_ERR_INVALID, "both the host and the device copy of the input are needed");
+        *job = submit(ctx, circuit, n_copies, grinding_bits, h_input, d_input, proof_out, proof_cap, claimed_v,
+                      marker_slot, nullptr);
     });
 }
 
@@ -1710,6 +1775,19 @@ int gkrgpu_memcpy_h2d(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t byte
             c.copy(dst, src, bytes, cudaMemcpyHostToDevice, "cudaMemcpyAsync");
             c.sync();
         });
+    });
+}
+
+int gkrgpu_upload(gkrgpu_ctx* ctx, void* d_dst, const void* h_src, uint64_t bytes) {
+    return guarded([&] {
+        check_ctx(ctx);
+        if (!d_dst || (!h_src && bytes)) fail(GKRGPU_ERR_INVALID, "null buffer");
+        std::lock_guard<std::mutex> lk(ctx->xfer_m);
+        DeviceGuard dg(ctx->device);
+        if (!ctx->xfer) ck(cudaStreamCreateWithFlags(&ctx->xfer, cudaStreamNonBlocking), "cudaStreamCreate");
+        ck(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, ctx->xfer), "cudaMemcpyAsync");
+        ck(cudaStreamSynchronize(ctx->xfer), "cudaStreamSynchronize");
+        ctx->h2d_bytes += bytes;
     });
 }
 

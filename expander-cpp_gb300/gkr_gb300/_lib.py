@@ -72,11 +72,13 @@ SIGNATURES = [
     ("gkrgpu_prove_device", _I, [_P, _P, _U32, _I, _P, _P, _U64, ctypes.POINTER(_U64), _P]),
     ("gkrgpu_prove_submit", _I, [_P, _P, _U32, _I, _P, _I, _P, _U64, _P, _I, ctypes.POINTER(_P)]),
     ("gkrgpu_prove_wait", _I, [_P, ctypes.POINTER(_U64)]),
+    ("gkrgpu_prove_submit_resident", _I, [_P, _P, _U32, _I, _P, _P, _P, _U64, _P, _I, ctypes.POINTER(_P)]),
     ("gkrgpu_verify", _I, [_P, _P, _U32, _I, _P, _U64, _P, ctypes.POINTER(_I)]),
     ("gkrgpu_set_fs_hash", _I, [_P, _I]),
     ("gkrgpu_keccak256", None, [_P, _U64, _P]),
     ("gkrgpu_sha3_256", None, [_P, _U64, _P]),
     ("gkrgpu_set_concurrency", _I, [_P, _I, _U64]),
+    ("gkrgpu_set_host_threads", _I, [_P, _I]),
     ("gkrgpu_workspace_bytes", _U64, [_P, _U32, _I, _I]),
     ("gkrgpu_memory_stats", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     ("gkrgpu_eval_multilinear", _I, [_P, _P, _U32, _U32, _P, _I, _P]),
@@ -87,6 +89,7 @@ SIGNATURES = [
     ("gkrgpu_host_free", _I, [_P]),
     ("gkrgpu_memcpy_h2d", _I, [_P, _P, _P, _U64]),
     ("gkrgpu_memcpy_d2h", _I, [_P, _P, _P, _U64]),
+    ("gkrgpu_upload", _I, [_P, _P, _P, _U64]),
     ("gkrgpu_set_timing", _I, [_P, _I]),
     ("gkrgpu_reset_stats", _I, [_P]),
     ("gkrgpu_kernel_stats", _I, [_P, _P, _I]),

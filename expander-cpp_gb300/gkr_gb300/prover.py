@@ -211,6 +211,28 @@ class Context:
                                            ctypes.byref(h)))
         return Job(h, (keep, proof_buf, claimed_buf))
 
+    def submit_resident(self, dc: DeviceCircuit, witness, d_input: int, proof_buf, claimed_buf, grinding_bits=10,
+                        marker=-1):
+        """gkrgpu_prove_submit_resident: the witness both in host memory (hashed for the RAW
+        commitment) and resident on the device at d_input (computed from); no input copy."""
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        keep = _table(dc.field, witness)
+        _lib.check(lib.gkrgpu_prove_submit_resident(self.handle, dc.handle, claimed_buf.shape[1], grinding_bits,
+                                                    keep.ctypes.data, ctypes.c_void_p(d_input),
+                                                    proof_buf.ctypes.data, proof_buf.nbytes, claimed_buf.ctypes.data,
+                                                    marker, ctypes.byref(h)))
+        return Job(h, (keep, proof_buf, claimed_buf))
+
+    def upload(self, d_dst: int, host_array):
+        """gkrgpu_upload: host -> device copy that does not wait for queued proofs."""
+        a = np.ascontiguousarray(host_array)
+        _lib.check(_lib.load().gkrgpu_upload(self.handle, ctypes.c_void_p(d_dst), a.ctypes.data, a.nbytes))
+
+    def set_host_threads(self, threads=0):
+        """Host threads for host stages (commitment hashing); 0 restores the default."""
+        _lib.check(_lib.load().gkrgpu_set_host_threads(self.handle, threads))
+
     def wait(self, job: "Job") -> int:
         """gkrgpu_prove_wait: blocks until the job is done; returns the proof length."""
         plen = ctypes.c_uint64()

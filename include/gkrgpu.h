@@ -204,6 +204,10 @@ typedef struct gkrgpu_job gkrgpu_job;
  * threads, so the sequential hashes of several queued proofs overlap.
  * No counterpart in the reference, which proves one circuit per thread. */
 int gkrgpu_set_concurrency(gkrgpu_ctx* ctx, int lanes, uint64_t hbm_budget_bytes);
+/* Host threads that run host stages (the SHA-256 of the RAW commitment, grinding): the
+ * hashes of queued proofs' commitments are sequential each, so this many run at once.  0
+ * restores the default, max(4, min(lanes, 8)).  Waits for queued proofs first. */
+int gkrgpu_set_host_threads(gkrgpu_ctx* ctx, int threads);
 /* Device bytes one proof of this circuit holds while it runs. */
 uint64_t gkrgpu_workspace_bytes(const gkrgpu_circuit* circuit, uint32_t n_copies, int grinding_bits,
                                 int input_on_device);
@@ -214,6 +218,16 @@ int gkrgpu_prove_submit(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t
                         const uint32_t* input, int input_on_device, uint8_t* proof_out, uint64_t proof_cap,
                         uint32_t* claimed_v, int marker_slot, gkrgpu_job** job);
 int gkrgpu_prove_wait(gkrgpu_job* job, uint64_t* proof_len);
+
+/* gkrgpu_prove_submit for an input held both in host memory and, resident, in device
+ * memory (16-byte aligned; the same values): the host stage copies and hashes the RAW
+ * commitment from h_input and the device stage computes from d_input, so nothing is copied
+ * between host and device for the input.  For request loops that upload each witness once,
+ * when it is admitted, and keep it on the device.  No counterpart in the reference. */
+int gkrgpu_prove_submit_resident(gkrgpu_ctx* ctx, const gkrgpu_circuit* circuit, uint32_t n_copies,
+                                 int grinding_bits, const uint32_t* h_input, const uint32_t* d_input,
+                                 uint8_t* proof_out, uint64_t proof_cap, uint32_t* claimed_v, int marker_slot,
+                                 gkrgpu_job** job);
 
 /* eval_multilinear (include/poly_commit/poly.hpp:88-104) of a device table d_evals of
  * 2^nb_vars rows at n_points (1..3) points: r is a host array of n_points x nb_vars
@@ -250,6 +264,10 @@ int gkrgpu_host_alloc(uint64_t bytes, void** out);
 int gkrgpu_host_free(void* p);
 int gkrgpu_memcpy_h2d(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t bytes);
 int gkrgpu_memcpy_d2h(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t bytes);
+/* Host -> device copy on the context's own transfer stream: unlike gkrgpu_memcpy_h2d it
+ * does not wait for queued proofs, which keep running while it copies; it returns when the
+ * copy is done.  For request loops that upload witnesses as requests are admitted. */
+int gkrgpu_upload(gkrgpu_ctx* ctx, void* d_dst, const void* h_src, uint64_t bytes);
 
 /* Launch accounting.  With timing on, every kernel launch is bracketed by CUDA events on
  * the context's stream.  Counts and times are added to the totals when each proof (or
@@ -257,8 +275,11 @@ int gkrgpu_memcpy_d2h(gkrgpu_ctx* ctx, void* dst, const void* src, uint64_t byte
  * flight, always reads whole proofs; it fills up to cap entries (one per kernel kind) and
  * returns how many kinds exist.  gkrgpu_set_timing and gkrgpu_reset_stats first wait for
  * queued proofs to finish.  When the environment variable GKRGPU_TRACE names a file at
- * gkrgpu_create, every timed launch also appends a CSV line to it: kernel kind, layer,
- * phase (0 evaluate, 1, 2), round, algorithmic bytes, milliseconds. */
+ * gkrgpu_create, every timed launch also appends a CSV line to it: kernel kind, lane,
+ * layer, phase (0 evaluate, 1, 2), round, algorithmic bytes, milliseconds, and the launch's
+ * device start and host launch-call time in milliseconds after the context's creation
+ * (plus a host_stage_wait line per proof: how long its device stage waited for the host
+ * stage). */
 int gkrgpu_set_timing(gkrgpu_ctx* ctx, int enabled);
 int gkrgpu_reset_stats(gkrgpu_ctx* ctx);
 int gkrgpu_kernel_stats(gkrgpu_ctx* ctx, gkrgpu_kernel_stat* out, int cap);
