@@ -34,7 +34,8 @@ namespace gkrgpu {
 const char* const kKernelNames[K_NUM_KERNELS] = {"check_canonical", "evaluate", "eq_table", "gate_weights",
                                                  "hg_build_round0", "round_fold_lane", "round_fold_scalar",
                                                  "phase2_s_build", "weighted_row_sum", "hg_rebuild_round1",
-                                                 "verifier_gate_sums", "canonicalize", "phase2_round0", "bn254_load",
+                                                 "verifier_gate_sums", "canonicalize", "phase2_round0", "stage_words",
+                                                 "bn254_load",
                                                  "bn254_evaluate", "bn254_eq_table", "bn254_gate_weights",
                                                  "bn254_hg_build_round0", "bn254_round_fold_lane",
                                                  "bn254_round_fold_scalar", "bn254_phase2_s_build",
@@ -157,6 +158,12 @@ __device__ __forceinline__ TileIdx tile_idx(const Geo& g) {
     return t;
 }
 
+// Index of the i-th group a kernel works on: with a list, its i-th entry (the groups that
+// have gates, in increasing order), otherwise i itself.
+__device__ __forceinline__ uint64_t group_at(const uint32_t* __restrict__ list, uint64_t i) {
+    return list ? (uint64_t)__ldg(list + i) : i;
+}
+
 // ---------------------------------------------------------------- input check
 __global__ void k_check_canonical(const uint32_t* __restrict__ v, uint64_t n, unsigned int* flag) {
     uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -165,7 +172,28 @@ __global__ void k_check_canonical(const uint32_t* __restrict__ v, uint64_t n, un
         uint4 x = __ldg(reinterpret_cast<const uint4*>(v) + i);
         bad |= (x.x >= m31::P) | (x.y >= m31::P) | (x.z >= m31::P) | (x.w >= m31::P);
     }
-    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+    // every writer stores the same 1, so a plain store works for device and host-mapped flags
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) *reinterpret_cast<volatile unsigned int*>(flag) = 1u;
+}
+
+// ---------------------------------------------------------------- small transfers
+// dst[k * n + i] = src_k[i] for i < n, k < nsrc: small tables moved between device memory and
+// host-mapped memory by the SMs, so a proof's stream never waits behind a bulk copy of another
+// proof on the copy engine.  With `done`, each CTA makes its writes visible to the host and
+// then increments the counter (system scope).
+__global__ void k_stage_words(uint32_t* dst, const uint32_t* s0, const uint32_t* s1, const uint32_t* s2, uint32_t nsrc,
+                              uint64_t n, unsigned int* done) {
+    const uint64_t total = n * nsrc, stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        const uint64_t k = i / n, e = i - k * n;
+        const uint32_t* src = k == 0 ? s0 : (k == 1 ? s1 : s2);
+        dst[i] = src[e];
+    }
+    if (done) {
+        __threadfence_system();
+        __syncthreads();
+        if (threadIdx.x == 0) atomicAdd_system(done, 1u);
+    }
 }
 
 // In-place M31::from_bytes of u32 words (the verifier reads the commitment from proof bytes).
@@ -396,7 +424,8 @@ constexpr int kStageFields = 5;  // v(2i), v(2i+1), a(2i), a(2i+1), (off(2i), of
 constexpr int kMaxStagedSmem = kStages * kStageFields * 16 * 256;
 
 template <int R>
-__global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict__ v, uint64_t I,
+__global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict__ v, uint64_t npairs,
+                                                      const uint32_t* __restrict__ pairs,
                                                       const uint32_t* __restrict__ mx_off,
                                                       const uint4* __restrict__ mx_g, const uint4* __restrict__ a4,
                                                       const uint4* __restrict__ w4, Geo g, RedScratch red,
@@ -449,26 +478,34 @@ __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict
         }
     };
     if (t.active) {
-        const uint64_t npairs = I >> 1, step = (uint64_t)gridDim.x * g.rps;
+        // iteration i works on pair q = group_at(pairs, i) (rows 2q, 2q+1); the list entry of
+        // the iteration staged next is loaded one iteration ahead of its staging
+        const uint64_t step = (uint64_t)gridDim.x * g.rps;
         const uint64_t i0 = (uint64_t)blockIdx.x * g.rps + t.rs;
-        auto stage = [&](uint64_t i, int slot) {
+        auto stage = [&](uint64_t i, uint64_t q, int slot) {
             if (i < npairs) {
                 uint4* st = ring + (size_t)slot * kStageFields * B + tid;
-                cp_async16(st, v + (2 * i) * g.N + t.lane0);
-                cp_async16(st + B, v + (2 * i + 1) * g.N + t.lane0);
-                cp_async16(st + 2 * B, a4 + 2 * i);
-                cp_async16(st + 3 * B, a4 + 2 * i + 1);
-                cp_async8(st + 4 * B, mx_off + 2 * i);
-                cp_async4(reinterpret_cast<uint32_t*>(st + 4 * B) + 2, mx_off + 2 * i + 2);
+                cp_async16(st, v + (2 * q) * g.N + t.lane0);
+                cp_async16(st + B, v + (2 * q + 1) * g.N + t.lane0);
+                cp_async16(st + 2 * B, a4 + 2 * q);
+                cp_async16(st + 3 * B, a4 + 2 * q + 1);
+                cp_async8(st + 4 * B, mx_off + 2 * q);
+                cp_async4(reinterpret_cast<uint32_t*>(st + 4 * B) + 2, mx_off + 2 * q + 2);
             }
             cp_async_commit();  // one group per iteration, empty past the end
         };
 #pragma unroll
-        for (int s = 0; s < kStages - 1; s++) stage(i0 + s * step, s);
+        for (int s = 0; s < kStages - 1; s++) {
+            const uint64_t i = i0 + s * step;
+            stage(i, i < npairs ? group_at(pairs, i) : 0, s);
+        }
+        uint64_t next_q = i0 + (kStages - 1) * step < npairs ? group_at(pairs, i0 + (kStages - 1) * step) : 0;
         int slot = 0;
         for (uint64_t i = i0; i < npairs; i += step) {
             // refill the slot read in the previous iteration, then wait for this one
-            stage(i + (kStages - 1) * step, slot == 0 ? kStages - 1 : slot - 1);
+            const uint64_t is = i + (kStages - 1) * step, q = next_q;
+            next_q = is + step < npairs ? group_at(pairs, is + step) : 0;
+            stage(is, q, slot == 0 ? kStages - 1 : slot - 1);
             cp_async_wait<kStages - 1>();
             const uint4* st = ring + (size_t)slot * kStageFields * B + tid;
             const uint4 f0 = st[0], f1 = st[B], off = st[4 * B];
@@ -510,6 +547,7 @@ __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict
 // after the first row of a pair only its f and h are kept, for pc.
 template <int R>
 __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ v, uint64_t npairs,
+                                                   const uint32_t* __restrict__ quads,
                                                    const uint32_t* __restrict__ mx_off, const uint4* __restrict__ mx_g,
                                                    const uint4* __restrict__ a4, const uint4* __restrict__ w4,
                                                    RoundPtrs p, Geo g, RedScratch red, uint32_t* evals_out) {
@@ -520,7 +558,13 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
 #pragma unroll
         for (int l = 0; l < 4; l++) acc[c][l] = 0u;
     if (t.active) {
-        for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
+        // iteration ii works on output pair i = group_at(quads, ii) (source rows 4i .. 4i+3)
+        const uint64_t step = (uint64_t)gridDim.x * g.rps;
+        uint64_t ii = (uint64_t)blockIdx.x * g.rps + t.rs;
+        uint64_t next_i = ii < npairs ? group_at(quads, ii) : 0;
+        for (; ii < npairs; ii += step) {
+            const uint64_t i = next_i;
+            next_i = ii + step < npairs ? group_at(quads, ii + step) : 0;
             const uint4 o4 = __ldg(reinterpret_cast<const uint4*>(mx_off + 4 * i));  // off(4i .. 4i+3)
             const uint32_t o_end = __ldg(mx_off + 4 * i + 4);
             const uint32_t off[5] = {o4.x, o4.y, o4.z, o4.w, o_end};
@@ -1106,8 +1150,9 @@ struct P01Fin {
 };
 
 template <int R>
-__global__ void __launch_bounds__(256, 2) k_p2_round01(P01Src src, uint64_t ngroups, const uint32_t* __restrict__ vx,
-                                                       Geo g, RedScratch red, uint32_t* evals_out, uint32_t* sums_out) {
+__global__ void __launch_bounds__(256, 2) k_p2_round01(P01Src src, uint64_t ngroups, const uint32_t* __restrict__ quads,
+                                                       const uint32_t* __restrict__ vx, Geo g, RedScratch red,
+                                                       uint32_t* evals_out, uint32_t* sums_out) {
     extern __shared__ uint4 ring01[];  // kP01Stages x warps x kP01WarpSlot bytes
     const uint32_t tid = threadIdx.x, wl = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
     const uint32_t L = g.tpr, rs = tid / L;  // L: copies per row slice, a multiple of 32
@@ -1130,21 +1175,29 @@ __global__ void __launch_bounds__(256, 2) k_p2_round01(P01Src src, uint64_t ngro
     if (active) {
         const uint64_t step = (uint64_t)gridDim.x * g.rps;
         const uint64_t i0 = (uint64_t)blockIdx.x * g.rps + rs;
-        auto stage = [&](uint64_t i, int slot) {
+        // iteration i works on row group q = group_at(quads, i) (rows 4q .. 4q+3); the list
+        // entry of the iteration staged next is loaded one iteration ahead of its staging
+        auto stage = [&](uint64_t i, uint64_t q, int slot) {
             if (i < ngroups) {
                 char* st = ring + ((size_t)slot * nw + w) * kP01WarpSlot;
-                cp_async16(st + 16 * wl, vst + 4 * i * N);
-                if (sst) cp_async16(st + 512 + 16 * wl, sst + 4 * i);
+                cp_async16(st + 16 * wl, vst + 4 * q * N);
+                if (sst) cp_async16(st + 512 + 16 * wl, sst + 4 * q);
             }
             cp_async_commit();  // one group per iteration, empty past the end
         };
 #pragma unroll
-        for (int s = 0; s < kP01Stages - 1; s++) stage(i0 + s * step, s);
+        for (int s = 0; s < kP01Stages - 1; s++) {
+            const uint64_t i = i0 + s * step;
+            stage(i, i < ngroups ? group_at(quads, i) : 0, s);
+        }
+        uint64_t next_q = i0 + (kP01Stages - 1) * step < ngroups ? group_at(quads, i0 + (kP01Stages - 1) * step) : 0;
         int slot = 0;
         uint32_t it = 0;
         for (uint64_t i = i0; i < ngroups; i += step, it++) {
             __syncwarp();  // every lane has read the slot refilled next
-            stage(i + (kP01Stages - 1) * step, slot == 0 ? kP01Stages - 1 : slot - 1);
+            const uint64_t is = i + (kP01Stages - 1) * step, q = next_q;
+            next_q = is + step < ngroups ? group_at(quads, is + step) : 0;
+            stage(is, q, slot == 0 ? kP01Stages - 1 : slot - 1);
             cp_async_wait<kP01Stages - 1>();
             __syncwarp();  // the other lanes' copies of this slot are visible
             const char* st = ring + ((size_t)slot * nw + w) * kP01WarpSlot;
@@ -1399,20 +1452,32 @@ static size_t hg0_smem(size_t ring_bytes, size_t red_bytes) {
     return ring_bytes > red_bytes ? ring_bytes : red_bytes;
 }
 
-cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint32_t* mx_off, const uint4* mx_g,
-                             const uint4* a4, const uint4* w4, const Geo& g, uint32_t block, uint32_t ctas,
-                             RedScratch red, uint32_t* evals_out, cudaStream_t s) {
+uint32_t launch_stage_words(uint32_t* dst, const uint32_t* const* srcs, uint32_t nsrc, uint64_t n, unsigned int* done,
+                            cudaStream_t s, cudaError_t* err) {
+    const uint64_t total = n * nsrc;
+    uint64_t ctas = (total + 256 * 16 - 1) / (256 * 16);
+    if (ctas < 1) ctas = 1;
+    if (ctas > 64) ctas = 64;
+    k_stage_words<<<(uint32_t)ctas, 256, 0, s>>>(dst, srcs[0], nsrc > 1 ? srcs[1] : nullptr,
+                                                 nsrc > 2 ? srcs[2] : nullptr, nsrc, n, done);
+    *err = cudaGetLastError();
+    return (uint32_t)ctas;
+}
+
+cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* pairs,
+                             const uint32_t* mx_off, const uint4* mx_g, const uint4* a4, const uint4* w4, const Geo& g,
+                             uint32_t block, uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
     // the kernel's launch bound is 256 threads: wider tiles are narrowed to it
     Geo gb = g;
     if (block > 256) block = 256;
     while (gb.tpr > block && gb.tpr % 2 == 0) gb.tpr /= 2;
     if (gb.tpr > block) return cudaErrorInvalidValue;
     gb.rps = block / gb.tpr;
-    LaunchShape sh = row_shape(gb, I / 2, block, ctas, 3 * reps);
+    LaunchShape sh = row_shape(gb, npairs, block, ctas, 3 * reps);
     const size_t ring = (size_t)kStages * kStageFields * sizeof(uint4) * block;
-#define GKR_HG0(RR)                                                                                          \
-    k_hg_round0<RR><<<sh.grid, sh.block, hg0_smem<RR>(ring, sh.smem), s>>>(v, I, mx_off, mx_g, a4, \
-                                                                                      w4, gb, red, evals_out)
+#define GKR_HG0(RR)                                                                                                \
+    k_hg_round0<RR><<<sh.grid, sh.block, hg0_smem<RR>(ring, sh.smem), s>>>(v, npairs, pairs, mx_off, mx_g, a4, w4, \
+                                                                          gb, red, evals_out)
     switch (reps) {
         case 1: GKR_HG0(1); break;
         case 2: GKR_HG0(2); break;
@@ -1423,16 +1488,21 @@ cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint
     return cudaGetLastError();
 }
 
-cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* mx_off, const uint4* mx_g,
-                             const uint4* a4, const uint4* w4, const RoundPtrs& p, const Geo& g, uint32_t block,
-                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
+cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* quads,
+                             const uint32_t* mx_off, const uint4* mx_g, const uint4* a4, const uint4* w4,
+                             const RoundPtrs& p, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
+                             uint32_t* evals_out, cudaStream_t s) {
+    if (quads && p.fdst[0]) return cudaErrorInvalidValue;  // stored folded copies need every pair
     LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
+#define GKR_HG1(RR) \
+    k_hg_round1<RR><<<sh.grid, sh.block, sh.smem, s>>>(v, npairs, quads, mx_off, mx_g, a4, w4, p, g, red, evals_out)
     switch (reps) {
-        case 1: k_hg_round1<1><<<sh.grid, sh.block, sh.smem, s>>>(v, npairs, mx_off, mx_g, a4, w4, p, g, red, evals_out); break;
-        case 2: k_hg_round1<2><<<sh.grid, sh.block, sh.smem, s>>>(v, npairs, mx_off, mx_g, a4, w4, p, g, red, evals_out); break;
-        case 3: k_hg_round1<3><<<sh.grid, sh.block, sh.smem, s>>>(v, npairs, mx_off, mx_g, a4, w4, p, g, red, evals_out); break;
+        case 1: GKR_HG1(1); break;
+        case 2: GKR_HG1(2); break;
+        case 3: GKR_HG1(3); break;
         default: return cudaErrorInvalidValue;
     }
+#undef GKR_HG1
     return cudaGetLastError();
 }
 
@@ -1552,8 +1622,8 @@ uint32_t p2_round01_groups(uint32_t N) {
 }
 
 cudaError_t launch_p2_round01(int reps, const uint32_t* v, const uint32_t* const* s, const uint32_t* const* t,
-                              uint64_t ngroups, const uint32_t* vx, uint32_t N, uint32_t ctas, RedScratch red,
-                              uint32_t* evals_out, uint32_t* sums_out, cudaStream_t st) {
+                              uint64_t ngroups, const uint32_t* quads, const uint32_t* vx, uint32_t N, uint32_t ctas,
+                              RedScratch red, uint32_t* evals_out, uint32_t* sums_out, cudaStream_t st) {
     if (reps < 1 || reps > 3 || p2_round01_groups(N) == 0) return cudaErrorInvalidValue;
     if ((reinterpret_cast<uintptr_t>(v) & 15) != 0) return cudaErrorInvalidValue;  // 16-byte cp.async
     Geo g;
@@ -1574,9 +1644,9 @@ cudaError_t launch_p2_round01(int reps, const uint32_t* v, const uint32_t* const
         src.t[j] = j < reps ? t[j] : nullptr;
     }
     switch (reps) {
-        case 1: k_p2_round01<1><<<grid, 256, smem, st>>>(src, ngroups, vx, g, red, evals_out, sums_out); break;
-        case 2: k_p2_round01<2><<<grid, 256, smem, st>>>(src, ngroups, vx, g, red, evals_out, sums_out); break;
-        default: k_p2_round01<3><<<grid, 256, smem, st>>>(src, ngroups, vx, g, red, evals_out, sums_out); break;
+        case 1: k_p2_round01<1><<<grid, 256, smem, st>>>(src, ngroups, quads, vx, g, red, evals_out, sums_out); break;
+        case 2: k_p2_round01<2><<<grid, 256, smem, st>>>(src, ngroups, quads, vx, g, red, evals_out, sums_out); break;
+        default: k_p2_round01<3><<<grid, 256, smem, st>>>(src, ngroups, quads, vx, g, red, evals_out, sums_out); break;
     }
     return cudaGetLastError();
 }

@@ -68,6 +68,7 @@ enum KernelId {
     K_GATE_SUMS,   // verifier
     K_CANONICAL,   // verifier
     K_P2_ROUND0,
+    K_STAGE,  // small transfers between device and host-mapped memory
     // BN254 kernels (bn254.cuh)
     K_BN_LOAD,
     K_BN_EVALUATE,
@@ -101,19 +102,30 @@ cudaError_t launch_evaluate(const uint32_t* in, uint32_t* out, uint64_t O, const
                             const uint32_t* ao_off, const uint2* ao_g, const Geo& g, uint32_t block, uint32_t ctas,
                             cudaStream_t s);
 cudaError_t launch_eq(uint32_t* out, const EqArgs& a, cudaStream_t s);
+// dst[k * n + i] = srcs[k][i] (nsrc <= 3 tables of n words) by a small kernel instead of the
+// copy engine, for transfers between device and host-mapped memory; with `done`, every CTA
+// increments it after its writes are visible to the host.  Returns the CTA count (the
+// number of increments); *err receives the launch status.
+uint32_t launch_stage_words(uint32_t* dst, const uint32_t* const* srcs, uint32_t nsrc, uint64_t n, unsigned int* done,
+                            cudaStream_t s, cudaError_t* err);
 cudaError_t launch_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* eqc, const uint4* mx_g,
                            const uint32_t* ax_off, const uint2* ax_g, uint4* a_out, uint4* w_out, uint32_t reps,
                            cudaStream_t s);
-// Phase-one hg (not stored) and the round-0 evaluations.
-cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t I, const uint32_t* mx_off, const uint4* mx_g,
-                             const uint4* a4, const uint4* w4, const Geo& g, uint32_t block, uint32_t ctas,
-                             RedScratch red, uint32_t* evals_out, cudaStream_t s);
+// Phase-one hg (not stored) and the round-0 evaluations over `npairs` pairs of input rows:
+// pair i is (2q, 2q+1) with q = pairs[i], or q = i without a list (pairs = null).  Pairs
+// left out of the list must have no gate whose first input is in them (their hg is zero).
+cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* pairs,
+                             const uint32_t* mx_off, const uint4* mx_g, const uint4* a4, const uint4* w4, const Geo& g,
+                             uint32_t block, uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
 // Phase-one round 1 rebuilding hg from the gate weights (no stored hg table): outputs
 // p.fdst[j] / p.hdst[j] (I/2 rows each; p.fdst[0] null: the folded copies are not stored),
-// challenges p.r[j]; npairs = I/4.
-cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* mx_off, const uint4* mx_g,
-                             const uint4* a4, const uint4* w4, const RoundPtrs& p, const Geo& g, uint32_t block,
-                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
+// challenges p.r[j]; npairs output pairs, pair i folding input rows 4q .. 4q+3 with
+// q = quads[i] (q = i without a list).  A list, which may leave out only groups of four rows
+// with no gate whose first input is in them, needs p.fdst[0] null.
+cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* quads,
+                             const uint32_t* mx_off, const uint4* mx_g, const uint4* a4, const uint4* w4,
+                             const RoundPtrs& p, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
+                             uint32_t* evals_out, cudaStream_t s);
 // Phase-one round 2 or 3 (k = round, a k_round with per-copy hg and fold) reading the
 // previous round's stored hg rows and recomputing the copy-independent ones (p.hoff, p.ha,
 // p.hr); round 2 in turn does not store its copy-independent output rows.
@@ -138,9 +150,11 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold, con
 // red.acc needs 9 * reps x N accumulators.  Publishes p2_round01_groups(N) lane groups;
 // p2_round01_groups(N) is 0 where the kernel does not apply (its row slices of up to 256
 // copies must be a multiple of 32 copies).
+// Groups i < ngroups are rows 4q .. 4q+3 with q = quads[i] (q = i without a list); a list
+// may leave out only groups with no mul gate whose second input is in them (s_j zero there).
 cudaError_t launch_p2_round01(int reps, const uint32_t* v, const uint32_t* const* s, const uint32_t* const* t,
-                              uint64_t ngroups, const uint32_t* vx, uint32_t N, uint32_t ctas, RedScratch red,
-                              uint32_t* evals_out, uint32_t* sums_out, cudaStream_t st);
+                              uint64_t ngroups, const uint32_t* quads, const uint32_t* vx, uint32_t N, uint32_t ctas,
+                              RedScratch red, uint32_t* evals_out, uint32_t* sums_out, cudaStream_t st);
 uint32_t p2_round01_groups(uint32_t N);
 // Phase-two round 1 from those sums at the round-0 challenges r[j]: evaluations to evals_out
 // (one completion count on done), and the scalar tables s[j] folded into sd[j] (2 ngroups

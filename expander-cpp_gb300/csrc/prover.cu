@@ -171,6 +171,13 @@ struct DevLayer {
     // the same after round 1: rows q < I/4 whose input rows 4q .. 4q+3 have no mul gates (not
     // stored by round 2, recomputed in round 3)
     uint64_t h2_scalar_rows = 0;
+    // Groups of input rows that have gates, for the kernels that skip the rest (the
+    // reference's gate_exists, sumcheck_helper.hpp:82-84,118-130): pairs (2q, 2q+1) and
+    // quads 4q .. 4q+3 with a gate whose first input is in them (phase one, rounds 0 and 1),
+    // quads with a mul gate whose second input is in them (phase two, rounds 0 and 1).  A
+    // null list means every group (used when nearly all of them have gates).
+    const uint32_t *p1_pairs = nullptr, *p1_quads = nullptr, *p2_quads = nullptr;
+    uint64_t n_p1_pairs = 0, n_p1_quads = 0, n_p2_quads = 0;
     // BN254 circuits: each gate's coefficient in Montgomery form, in the order of the table above
     const bn::Fr *mo_c = nullptr, *ao_c = nullptr, *mx_c = nullptr, *ax_c = nullptr, *my_c = nullptr;
     void* block = nullptr;
@@ -240,22 +247,29 @@ struct Lane {
     uint64_t job_launches[K_NUM_KERNELS] = {};
     double job_bytes[K_NUM_KERNELS] = {};
 
-    // Host-mapped staging for the round evaluations written by the finishing CTAs, followed
-    // by the completion counter they increment (RedScratch::done).
+    // Host-mapped staging: the round evaluations written by the finishing CTAs, then an extra
+    // area for the other small transfers of a proof (rows, claims, vx, the input check flag;
+    // moved by kernels, so the lane's stream never queues behind another proof's bulk copies
+    // on the copy engine), then the completion counter the kernels increment (RedScratch::done).
     char* map_h = nullptr;
     char* map_d = nullptr;
-    size_t map_cap = 0;
+    size_t map_cap = 0, map_extra = 0;
     uint32_t done_seen = 0;
     uint32_t* evals_h() const { return reinterpret_cast<uint32_t*>(map_h); }
     uint32_t* evals_d() const { return reinterpret_cast<uint32_t*>(map_d); }
+    char* extra_h() const { return map_h + map_extra; }
+    char* extra_d() const { return map_d + map_extra; }
     unsigned int* done_d() const { return reinterpret_cast<unsigned int*>(map_d + map_cap - 256); }
     volatile uint32_t* done_h() const { return reinterpret_cast<volatile uint32_t*>(map_h + map_cap - 256); }
-    void ensure_mapped(size_t evals_bytes) {
-        const size_t need = align_up(evals_bytes, 256) + 256;
-        if (need <= map_cap) return;
+    // The stream must be idle (a new block resets the counter).
+    void ensure_mapped(size_t evals_bytes, size_t extra_bytes = 0) {
+        const size_t ev = align_up(evals_bytes, 256), ex = align_up(extra_bytes, 256);
+        if (map_h && ev <= map_extra && map_extra + ex + 256 <= map_cap) return;
+        const size_t ev_new = std::max(ev, map_extra), ex_new = std::max(ex, map_h ? map_cap - 256 - map_extra : 0);
+        const size_t need = ev_new + ex_new + 256;
         if (map_h) cudaFreeHost(map_h);
         map_h = map_d = nullptr;
-        map_cap = 0;
+        map_cap = map_extra = 0;
         void* p = nullptr;
         ck(cudaHostAlloc(&p, need, cudaHostAllocMapped | cudaHostAllocPortable), "mapped staging allocation");
         map_h = static_cast<char*>(p);
@@ -263,6 +277,7 @@ struct Lane {
         ck(cudaHostGetDevicePointer(&d, p, 0), "cudaHostGetDevicePointer");
         map_d = static_cast<char*>(d);
         map_cap = need;
+        map_extra = ev_new;
         memset(map_h, 0, need);
         done_seen = 0;
     }
@@ -592,12 +607,31 @@ DevLayer upload_layer(const gkrgpu_layer_desc& d, int field) {
         if (bn) ax_c[k] = ca[ord[k]];
     }
 
+    // groups with gates (see DevLayer); a list is kept only when it leaves out more than a
+    // tenth of the groups, since walking it costs a dependent load per group
+    std::vector<uint32_t> l_p1_pairs, l_p1_quads, l_p2_quads;
+    if (!bn) {
+        auto gated = [](const std::vector<uint32_t>& off, uint64_t a, uint64_t b) { return off[b] > off[a]; };
+        for (uint64_t q = 0; q < I / 2; q++)
+            if (gated(off_mx, 2 * q, 2 * q + 2) || gated(off_ax, 2 * q, 2 * q + 2)) l_p1_pairs.push_back((uint32_t)q);
+        for (uint64_t q = 0; q < I / 4; q++) {
+            if (gated(off_mx, 4 * q, 4 * q + 4) || gated(off_ax, 4 * q, 4 * q + 4)) l_p1_quads.push_back((uint32_t)q);
+            if (gated(off_my, 4 * q, 4 * q + 4)) l_p2_quads.push_back((uint32_t)q);
+        }
+    }
+    const bool use_p1p = l_p1_pairs.size() * 10 <= (I / 2) * 9;
+    const bool use_p1q = l_p1_quads.size() * 10 <= (I / 4) * 9;
+    const bool use_p2q = l_p2_quads.size() * 10 <= (I / 4) * 9;
+
     struct Part {
         const void* src;
         size_t bytes;
         void** dst;
     };
     DevLayer L;
+    L.n_p1_pairs = use_p1p ? l_p1_pairs.size() : I / 2;
+    L.n_p1_quads = use_p1q ? l_p1_quads.size() : I / 4;
+    L.n_p2_quads = use_p2q ? l_p2_quads.size() : I / 4;
     L.h1_scalar_rows = h1_scalar;
     L.h2_scalar_rows = h2_scalar;
     L.nin = d.nb_input_vars;
@@ -611,6 +645,9 @@ DevLayer upload_layer(const gkrgpu_layer_desc& d, int field) {
         {off_ax.data(), off_ax.size() * 4, (void**)&L.ax_off}, {ax.data(), Ga * 8, (void**)&L.ax_g},
         {off_my.data(), off_my.size() * 4, (void**)&L.my_off}, {my.data(), Gm * 16, (void**)&L.my_g},
     };
+    if (!bn && use_p1p) parts.push_back({l_p1_pairs.data(), l_p1_pairs.size() * 4, (void**)&L.p1_pairs});
+    if (!bn && use_p1q) parts.push_back({l_p1_quads.data(), l_p1_quads.size() * 4, (void**)&L.p1_quads});
+    if (!bn && use_p2q) parts.push_back({l_p2_quads.data(), l_p2_quads.size() * 4, (void**)&L.p2_quads});
     if (bn) {
         parts.push_back({mo_c.data(), Gm * 32, (void**)&L.mo_c});
         parts.push_back({ao_c.data(), Ga * 32, (void**)&L.ao_c});
@@ -757,6 +794,26 @@ struct Prover {
     RedScratch red() const { return RedScratch{ws.acc, ws.ticket}; }
     // Round kernels publish their evaluations into the lane's mapped staging buffer.
     RedScratch red_mapped() const { return RedScratch{ws.acc, ws.ticket, c.done_d()}; }
+    // The lane's mapped extra area: rows 0..1 of each repetition's last table (6N words), the
+    // claims (3N), vx (3N) and the input check flag.
+    uint32_t* mapped(bool dev, uint64_t word) const {
+        return reinterpret_cast<uint32_t*>(dev ? c.extra_d() : c.extra_h()) + word;
+    }
+    uint32_t* rows_h() const { return mapped(false, 0); }
+    uint32_t* cv_h() const { return mapped(false, 6ull * N); }
+    uint32_t* vx_h() const { return mapped(false, 9ull * N); }
+    volatile uint32_t* flag_h() const { return mapped(false, 12ull * N); }
+    // Moves nsrc tables of n words into dst with k_stage_words (launch accounting as stage_words);
+    // returns the number of completion increments when `done` is given.
+    uint32_t stage(uint32_t* dst, const uint32_t* const* srcs, uint32_t nsrc, uint64_t n, unsigned int* done) {
+        uint32_t incs = 0;
+        c.launch(K_STAGE, 8.0 * n * nsrc, [&] {
+            cudaError_t e;
+            incs = launch_stage_words(dst, srcs, nsrc, n, done, c.stream, &e);
+            return e;
+        });
+        return done ? incs : 0;
+    }
     uint32_t groups(int kid) const { return N / (4 * gk[kid].tpr); }
 
     void reserve(bool own_input, bool sumcheck) {
@@ -766,12 +823,8 @@ struct Prover {
         block = static_cast<char*>(p);
         ws.plan(block, C, N, R, own_input, sumcheck);
         ck(cudaMemsetAsync(block + ws.zero_off, 0, ws.zero_bytes, c.stream), "cudaMemsetAsync");
-        c.ensure_mapped(9ull * N * 4);
+        c.ensure_mapped(9ull * N * 4, 12ull * N * 4 + 64);
         c.resync_done();
-        c.h_rows.ensure(6ull * N * 4, "pinned rows");
-        c.h_vx.ensure(3ull * N * 4, "pinned vx");
-        c.h_cv.ensure(3ull * N * 4, "pinned claims");
-        c.h_flag.ensure(4, "pinned flag");
     }
 
     void layout_values(const uint32_t* d_input) {
@@ -789,13 +842,16 @@ struct Prover {
         }
     }
 
+    // The check writes its flag straight into mapped memory; the host reads it after the
+    // stream has passed the claims (require_canonical).
     void check_input() {
         const uint64_t n = C.in_rows(0) * N;
-        c.launch(K_CHECK, (double)n * 4, [&] { return launch_check_canonical(vals[0], n, ws.flag, c.stream); });
-        c.copy(c.h_flag.p, ws.flag, 4, cudaMemcpyDeviceToHost, "input check readback");
+        *flag_h() = 0u;
+        std::atomic_thread_fence(std::memory_order_seq_cst);
+        c.launch(K_CHECK, (double)n * 4, [&] { return launch_check_canonical(vals[0], n, mapped(true, 12ull * N), c.stream); });
     }
     void require_canonical() {
-        if (*c.h_flag.as<unsigned>()) fail(GKRGPU_ERR_INVALID, "input contains a value >= 2^31 - 1");
+        if (*flag_h()) fail(GKRGPU_ERR_INVALID, "input contains a value >= 2^31 - 1");
     }
 
     void evaluate() {
@@ -812,17 +868,16 @@ struct Prover {
     }
 
     // Waits for the round's 3R evaluation rows (published by `groups` finishing CTAs into the
-    // mapped staging buffer) and optionally D2H-copies rows 0..1 of `rows_from` per repetition.
+    // mapped staging buffer) and optionally for rows 0..1 of `rows_from` per repetition, which
+    // a small kernel publishes into the mapped rows area the same way.
     void fetch(uint32_t groups, const uint32_t* const* rows_from, bool shared_rows) {
-        const uint64_t rowb = (uint64_t)N * 4;
+        uint32_t more = 0;
         if (rows_from) {
-            for (int j = 0; j < R; j++) {
-                const uint32_t* src = shared_rows ? rows_from[0] : rows_from[j];
-                c.copy(c.h_rows.as<char>() + 2 * j * rowb, src, 2 * rowb, cudaMemcpyDeviceToHost, "fetch rows");
-            }
+            const uint32_t* srcs[3];
+            for (int j = 0; j < R; j++) srcs[j] = shared_rows ? rows_from[0] : rows_from[j];
+            more = stage(mapped(true, 0), srcs, (uint32_t)R, 2ull * N, c.done_d());
         }
-        c.wait_done(groups);
-        if (rows_from) c.sync();
+        c.wait_done(groups + more);
     }
 
     // Transcript step of one round for every repetition (sumcheck.hpp:74-96).  With
@@ -845,7 +900,7 @@ struct Prover {
             const uint32_t r = t.challenge();
             rch[j][k] = r;
             if (last) {
-                const uint32_t* f0 = reinterpret_cast<const uint32_t*>(c.h_rows.as<char>() + 2 * j * rowb);
+                const uint32_t* f0 = rows_h() + 2ull * j * N;
                 const uint32_t* f1 = f0 + N;
                 uint32_t* dst = last_out + (uint64_t)j * N;
                 for (uint32_t i = 0; i < N; i++) dst[i] = m31::fold(f0[i], f1[i], r);
@@ -876,7 +931,7 @@ struct Prover {
         const uint64_t rowb = (uint64_t)N * 4;
         const double rb = 4.0 * N;
         uint32_t* v = vals[li];
-        uint32_t* vxh = c.h_vx.as<uint32_t>();
+        uint32_t* vxh = vx_h();
         std::vector<uint32_t> vy((size_t)R * N);
 
         // phase one: eqc_j = alpha eq(rz1_j) + beta eq(rz2_j), gate weights, hg + round 0
@@ -888,10 +943,13 @@ struct Prover {
         });
         // round 0 only reduces hg; round 1 rebuilds it (k_hg_round1), so no full-width hg
         // table is ever written
-        const double hb = rb * (I + Ly.nmul) + 32.0 * Ly.nmul + 20.0 * I;
+        // pairs of input rows without gates have hg = 0 and are skipped
+        const double np0 = (double)Ly.n_p1_pairs;
+        const double hb = rb * (2.0 * np0 + Ly.nmul) + 32.0 * Ly.nmul + 44.0 * np0;
         c.launch(K_HG_ROUND0, hb, [&] {
-            return launch_hg_round0(R, v, I, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, gk[K_HG_ROUND0], X.block,
-                                    ck_ctas[K_HG_ROUND0], red_mapped(), c.evals_d(), c.stream);
+            return launch_hg_round0(R, v, Ly.n_p1_pairs, Ly.p1_pairs, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4,
+                                    gk[K_HG_ROUND0], X.block, ck_ctas[K_HG_ROUND0], red_mapped(), c.evals_d(),
+                                    c.stream);
         });
         const uint32_t* vsrc[1] = {v};
         fetch(groups(K_HG_ROUND0), n == 1 ? vsrc : nullptr, true);
@@ -922,8 +980,13 @@ struct Prover {
                 if (refold1)
                     for (int j = 0; j < R; j++) p.fdst[j] = nullptr;
                 const double f_out = refold1 ? 0.0 : (double)R * I / 2;
-                c.launch(K_HG_ROUND1, rb * (I + Ly.nmul + f_out + (double)R * I / 2 - (double)R * Ly.h1_scalar_rows) + 32.0 * Ly.nmul + 20.0 * I, [&] {
-                    return launch_hg_round1(R, v, npairs, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, p, gk[K_HG_ROUND1],
+                // without stored folded copies, groups of four input rows without gates
+                // (hg = 0) are skipped
+                const uint32_t* quads = refold1 ? Ly.p1_quads : nullptr;
+                const uint64_t nq = refold1 ? Ly.n_p1_quads : npairs;
+                const double vin = 4.0 * nq;
+                c.launch(K_HG_ROUND1, rb * (vin + Ly.nmul + f_out + (double)R * I / 2 - (double)R * Ly.h1_scalar_rows) + 32.0 * Ly.nmul + 20.0 * vin, [&] {
+                    return launch_hg_round1(R, v, nq, quads, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, p, gk[K_HG_ROUND1],
                                             X.block, ck_ctas[K_HG_ROUND1], red_mapped(), c.evals_d(), c.stream);
                 });
             } else if (k == 2 || k == 3) {
@@ -982,15 +1045,20 @@ struct Prover {
                                     : launch_s_build(I, O, Ly.my_off, Ly.my_g, ws.eqc, ws.eqrx, ws.sb[0], sstride,
                                                      R, c.stream);
                  });
-        c.copy(ws.vx, vxh, R * rowb, cudaMemcpyHostToDevice, "vx upload");
+        {
+            const uint32_t* src[1] = {mapped(true, 9ull * N)};
+            stage(ws.vx, src, 1, (uint64_t)R * N, nullptr);
+        }
         uint32_t k_first = 1;
         if (fused01) {
             const uint64_t ngroups = I / 4;
             const uint32_t* sj[3] = {ws.sb[0], ws.sb[0] + sstride, ws.sb[0] + 2 * sstride};
             const uint32_t* tj[3] = {ws.sb[1], ws.sb[1] + sstride, ws.sb[1] + 2 * sstride};
-            c.launch(K_P2_ROUND0, rb * I + 8.0 * R * I + 4.0 * 9 * R * N, [&] {
-                return launch_p2_round01(R, v, sj, tj, ngroups, ws.vx, N, ck_ctas[K_P2_ROUND0], red_mapped(),
-                                         c.evals_d(), ws.p2s, c.stream);
+            // groups of four rows without mul gates on their second input (s = 0) are skipped
+            const double rows2 = 4.0 * Ly.n_p2_quads;
+            c.launch(K_P2_ROUND0, rb * rows2 + 8.0 * R * rows2 + 4.0 * 9 * R * N, [&] {
+                return launch_p2_round01(R, v, sj, tj, Ly.n_p2_quads, Ly.p2_quads, ws.vx, N, ck_ctas[K_P2_ROUND0],
+                                         red_mapped(), c.evals_d(), ws.p2s, c.stream);
             });
             fetch(p2_round01_groups(N), nullptr, true);
             transcript_round(t, ry, 0, false, false, vy.data());
@@ -1093,12 +1161,12 @@ struct Prover {
         eq_table(ws.eqc, rz1, nullptr, 1u, 0u, nz);
         const uint64_t OL = C.out_rows(L - 1);
         c.launch(K_WSUM, 4.0 * N * OL + 4.0 * R * OL, [&] {
-            return launch_wsum(R, vals[L], OL, ws.eqc, gk[K_WSUM], X.block, ck_ctas[K_WSUM], red(), ws.cv, c.stream);
+            return launch_wsum(R, vals[L], OL, ws.eqc, gk[K_WSUM], X.block, ck_ctas[K_WSUM], red(),
+                               mapped(true, 6ull * N), c.stream);
         });
-        c.copy(c.h_cv.p, ws.cv, R * rowb, cudaMemcpyDeviceToHost, "claims readback");
         c.sync();
         require_canonical();
-        memcpy(claimed_v, c.h_cv.p, R * rowb);
+        memcpy(claimed_v, cv_h(), R * rowb);
 
         for (int li = (int)L - 1; li >= 0; li--) {
             sumcheck_layer(t, (size_t)li, rz1, rz2, alpha, beta, rx, ry);
@@ -1202,10 +1270,36 @@ TranscriptState host_stage(gkrgpu_ctx& c, gkrgpu_job& j, cudaStream_t s) {
     if (j.h_input) {
         parallel_copy_and_hash(j.proof_out, reinterpret_cast<const uint8_t*>(j.h_input), in_bytes, j.fs_hash, d);
     } else {
-        ck(cudaMemcpyAsync(j.proof_out, j.d_input, in_bytes, cudaMemcpyDeviceToHost, s), "commitment readback");
-        ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        // the commitment is read back in chunks; SHA-256 hashes each chunk as it lands
+        const uint64_t chunk = 64ull << 20, nch = (in_bytes + chunk - 1) / chunk;
+        std::vector<cudaEvent_t> evs(nch, nullptr);
+        struct Evs {
+            std::vector<cudaEvent_t>& v;
+            ~Evs() {
+                for (auto e : v)
+                    if (e) cudaEventDestroy(e);
+            }
+        } guard{evs};
+        const uint8_t* src = reinterpret_cast<const uint8_t*>(j.d_input);
+        for (uint64_t k = 0; k < nch; k++) {
+            const uint64_t a = k * chunk, n = std::min(chunk, in_bytes - a);
+            ck(cudaEventCreateWithFlags(&evs[k], cudaEventDisableTiming), "cudaEventCreate");
+            ck(cudaMemcpyAsync(j.proof_out + a, src + a, n, cudaMemcpyDeviceToHost, s), "commitment readback");
+            ck(cudaEventRecord(evs[k], s), "cudaEventRecord");
+        }
+        if (j.fs_hash == kFsSha256) {
+            Sha256 h;
+            for (uint64_t k = 0; k < nch; k++) {
+                const uint64_t a = k * chunk, n = std::min(chunk, in_bytes - a);
+                ck(cudaEventSynchronize(evs[k]), "commitment readback");
+                h.update(j.proof_out + a, n);
+            }
+            h.final(d);
+        } else {
+            ck(cudaStreamSynchronize(s), "commitment readback");
+            fs_hash(j.fs_hash, j.proof_out, in_bytes, d);
+        }
         c.d2h_bytes += in_bytes;
-        fs_hash(j.fs_hash, j.proof_out, in_bytes, d);
     }
     Transcript t(j.proof_out, ~0ull, j.fs_hash);
     t.appended_prehashed(in_bytes, d);

@@ -179,3 +179,20 @@ def test_device_input_pipeline(ctx):
         n = ctx.wait(job)
         assert sha(pb[:n].tobytes()) == GOLDEN["lanes256"]["proof_sha256"]
     assert ctx.elapsed_ms(0, 1) >= 0.0
+
+
+@pytest.mark.parametrize("seed,widths,n", [
+    (401, [14, 10, 14, 9, 12], 32), (402, [16, 11, 15], 16), (403, [13, 8, 13, 6], 96), (404, [12, 9, 12], 1024),
+    (405, [15, 12, 15], 160),
+])
+def test_gpu_sparse_layers_skip_groups_without_gates(ctx, oracle, seed, widths, n):
+    """Layers much wider than their outputs: most pairs and quads of input rows are the first
+    input of no gate, and most quads the second input of no mul gate.  Phase one's rounds 0
+    and 1 and phase two's fused rounds 0 and 1 walk only the groups that have gates (their
+    sums over the others are zero); the proof must be the oracle's."""
+    circ = gc.random_circuit(seed, widths, p_mul=0.6, p_local=0.5, window=256)
+    w = gc.random_witness(seed, circ.log_input_size, n)
+    cv, proof = ctx.prove(ctx.load(circ), w)
+    ocv, oproof = oracle.prove(circ, w)
+    assert proof == oproof
+    assert np.array_equal(cv, ocv)
