@@ -34,7 +34,7 @@ namespace gkrgpu {
 const char* const kKernelNames[K_NUM_KERNELS] = {"check_canonical", "evaluate", "eq_table", "gate_weights",
                                                  "hg_build_round0", "round_fold_lane", "round_fold_scalar",
                                                  "phase2_s_build", "weighted_row_sum", "hg_rebuild_round1",
-                                                 "verifier_gate_sums", "canonicalize", "phase2_round0", "stage_words",
+                                                 "verifier_gate_sums", "canonicalize", "phase2_round0", "stage_words", "round_tail",
                                                  "bn254_load",
                                                  "bn254_evaluate", "bn254_eq_table", "bn254_gate_weights",
                                                  "bn254_hg_build_round0", "bn254_round_fold_lane",
@@ -634,6 +634,185 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
         }
     }
     reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R, true});
+}
+
+// ---------------------------------------------------------------- persistent phase tail
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ uint32_t ld_acquire_sys(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.sys.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+// Loads that see this kernel's own earlier writes (L2, not the non-coherent read-only path).
+__device__ __forceinline__ uint4 ld4cg(const uint32_t* base, uint64_t row, uint32_t N, uint32_t lane0) {
+    return __ldcg(reinterpret_cast<const uint4*>(base + row * N + lane0));
+}
+
+// The fold and sums of a round are those of k_round<false, LANE_HG, true> (receive_challenge
+// + poly_eval_at, sumcheck_helper.hpp:68-133) over this CTA's lane group and every row.
+template <bool LANE_HG>
+__global__ void __launch_bounds__(256) k_tail(TailArgs a) {
+    extern __shared__ uint32_t tsm[];
+    __shared__ uint32_t rch[3];
+    __shared__ int stop;
+    const Geo g = a.g;
+    const TileIdx t = tile_idx(g);
+    const uint32_t R = a.reps, tid = threadIdx.x, B = blockDim.x, tpr = g.tpr, rps = g.rps;
+    const uint32_t S0 = 1u << (a.n - a.kt + 1);  // rows of the first round's source tables
+    // shared memory: phase two's scalar tables (two buffers of R x S0), the reduction scratch
+    // (12 x B), the totals (R x 12 x tpr)
+    uint32_t* sbuf = tsm;
+    uint32_t* red = tsm + (LANE_HG ? 0 : 2 * 3 * S0);
+    uint32_t* tot = red + 12 * B;
+    if (tid == 0) stop = 0;
+    if (!LANE_HG) {
+        // every CTA keeps its own copy of the scalar tables (the source of round kt)
+        for (uint32_t j = 0; j < R; j++) {
+            const uint32_t* src = (a.kt & 1) ? a.hB[j] : a.hA[j];
+            for (uint32_t e = tid; e < S0; e += B) sbuf[j * S0 + e] = src[e];
+        }
+    }
+    __syncthreads();
+    for (uint32_t k = a.kt; k < a.n; k++) {
+        if (k == a.kt) {
+            if (tid < 3) rch[tid] = a.r_first[tid];
+        } else if (tid == 0) {
+            const uint32_t want = a.tag_base + (k - 1);
+            const uint32_t* slot = a.mbox + 4 + 4 * (k - 1);
+            const uint64_t t0 = global_ns();
+            uint32_t ns = 32;
+            int st = 0;
+            while (ld_acquire_sys(slot) != want) {
+                if (ld_acquire_sys(a.mbox) != 0) {
+                    st = 1;
+                    break;
+                }
+                if (global_ns() - t0 > a.wait_ns) {
+                    st = 2;
+                    break;
+                }
+                __nanosleep(ns);
+                if (ns < 1024) ns *= 2;
+            }
+            if (st == 2) *reinterpret_cast<volatile unsigned int*>(a.err) = 1u;
+            if (st == 0)
+                for (int j = 0; j < 3; j++) rch[j] = reinterpret_cast<const volatile uint32_t*>(slot)[1 + j];
+            stop = st;
+        }
+        __syncthreads();
+        if (stop) return;
+        const uint64_t npairs = 1ull << (a.n - k - 1);
+        const bool odd = k & 1;
+        // phase two: scalar tables ping-pong in shared memory (source of round kt in buffer 0)
+        const uint32_t* ssrc = sbuf + ((k - a.kt) & 1) * 3 * S0;
+        uint32_t* sdst = sbuf + (((k - a.kt) & 1) ^ 1) * 3 * S0;
+        uint32_t acc[3][3][4];
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+#pragma unroll
+                for (int l = 0; l < 4; l++) acc[j][c][l] = 0u;
+        if (t.active) {
+            for (uint64_t i = t.rs; i < npairs; i += rps) {
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    if ((uint32_t)j >= R) break;
+                    const uint32_t r = rch[j];
+                    const uint32_t* fs = odd ? a.fB[j] : a.fA[j];
+                    uint32_t* fd = odd ? a.fA[j] : a.fB[j];
+                    uint32_t f0[4], f1[4], h0[4], h1[4];
+                    uint4 x[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) x[q] = ld4cg(fs, 4 * i + q, g.N, t.lane0);
+                    if (LANE_HG) {
+                        const uint32_t* hs = odd ? a.hB[j] : a.hA[j];
+                        uint32_t* hd = odd ? a.hA[j] : a.hB[j];
+                        uint4 y[4];
+#pragma unroll
+                        for (int q = 0; q < 4; q++) y[q] = ld4cg(hs, 4 * i + q, g.N, t.lane0);
+#pragma unroll
+                        for (int l = 0; l < 4; l++) {
+                            h0[l] = fold(comp(y[0], l), comp(y[1], l), r);
+                            h1[l] = fold(comp(y[2], l), comp(y[3], l), r);
+                        }
+                        st4(hd, 2 * i, g.N, t.lane0, mk4(h0));
+                        st4(hd, 2 * i + 1, g.N, t.lane0, mk4(h1));
+                    } else {
+                        const uint32_t* sv = ssrc + j * S0 + 4 * i;
+                        const uint32_t s0 = fold(sv[0], sv[1], r), s1 = fold(sv[2], sv[3], r);
+                        if (t.q == 0) {
+                            sdst[j * S0 + 2 * i] = s0;
+                            sdst[j * S0 + 2 * i + 1] = s1;
+                        }
+#pragma unroll
+                        for (int l = 0; l < 4; l++) {
+                            h0[l] = s0;
+                            h1[l] = s1;
+                        }
+                    }
+#pragma unroll
+                    for (int l = 0; l < 4; l++) {
+                        f0[l] = fold(comp(x[0], l), comp(x[1], l), r);
+                        f1[l] = fold(comp(x[2], l), comp(x[3], l), r);
+                    }
+                    st4(fd, 2 * i, g.N, t.lane0, mk4(f0));
+                    st4(fd, 2 * i + 1, g.N, t.lane0, mk4(f1));
+                    accum_pair(acc[j], f0, f1, h0, h1);
+                }
+            }
+        }
+        // totals per (repetition, component, lane) over the CTA's row slices
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            if ((uint32_t)j >= R) break;
+            __syncthreads();
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+#pragma unroll
+                for (int l = 0; l < 4; l++) red[(c * 4 + l) * B + tid] = t.active ? acc[j][c][l] : 0u;
+            __syncthreads();
+            for (uint32_t o = tid; o < 12 * tpr; o += B) {
+                const uint32_t cl = o / tpr, q = o - cl * tpr;
+                unsigned long long sum = 0;
+                for (uint32_t rr = 0; rr < rps; rr++) sum += red[cl * B + rr * tpr + q];
+                tot[(j * 12 + cl) * tpr + q] = reduce64(sum);
+            }
+        }
+        __syncthreads();
+        // evaluations at 0, 1, 2 of every repetition for this group's lanes (RoundFin)
+        const uint32_t lanes = 4 * tpr, lane_base = blockIdx.y * lanes;
+        for (uint32_t li = tid; li < lanes; li += B) {
+            const uint32_t q = li >> 2, l = li & 3, lane = lane_base + li;
+            for (uint32_t j = 0; j < R; j++) {
+                uint32_t p0 = tot[(j * 12 + 0 * 4 + l) * tpr + q];
+                uint32_t p1 = tot[(j * 12 + 1 * 4 + l) * tpr + q];
+                const uint32_t c2 = tot[(j * 12 + 2 * 4 + l) * tpr + q];
+                uint32_t p2 = m31::eval_at_two(p0, p1, c2);
+                if (!LANE_HG) {
+                    const uint32_t xv = a.vx[(size_t)j * g.N + lane];
+                    p0 = mul(p0, xv);
+                    p1 = mul(p1, xv);
+                    p2 = mul(p2, xv);
+                }
+                a.evals_out[(size_t)(3 * j) * g.N + lane] = p0;
+                a.evals_out[(size_t)(3 * j + 1) * g.N + lane] = p1;
+                a.evals_out[(size_t)(3 * j + 2) * g.N + lane] = p2;
+                if (k + 1 == a.n) {
+                    const uint32_t* fd = odd ? a.fA[j] : a.fB[j];
+                    a.rows_out[(size_t)(2 * j) * g.N + lane] = __ldcg(fd + lane);
+                    a.rows_out[(size_t)(2 * j + 1) * g.N + lane] = __ldcg(fd + g.N + lane);
+                }
+            }
+        }
+        __threadfence_system();
+        __syncthreads();
+        if (tid == 0) atomicAdd_system(a.done, 1u);
+    }
 }
 
 // ---------------------------------------------------------------- fold + reduce round
@@ -1380,10 +1559,15 @@ LaunchShape rep_shape(const Geo& g, uint64_t rows, uint32_t block, uint32_t ctas
 
 }  // namespace
 
+// Row iterations a thread of a reducing kernel makes at least (when the table has that many
+// rows): each CTA ends with a reduction epilogue (shared-memory sums, one 64-bit atomic per
+// component and copy, the last-CTA finisher), which small grids pay less often.
+constexpr uint32_t kMinRowIters = 4;
+
 LaunchShape row_shape(const Geo& g, uint64_t rows, uint32_t block, uint32_t ctas_cap, uint32_t smem_components) {
     LaunchShape s;
     const uint32_t groups = g.N / (4 * g.tpr);
-    uint64_t need = (rows + g.rps - 1) / g.rps;
+    uint64_t need = (rows + (uint64_t)g.rps * kMinRowIters - 1) / ((uint64_t)g.rps * kMinRowIters);
     uint64_t cap = ctas_cap / groups;
     if (cap < 1) cap = 1;
     if (need < 1) need = 1;
@@ -1450,6 +1634,44 @@ static size_t hg0_smem(size_t ring_bytes, size_t red_bytes) {
         opted.fetch_or(bit);
     }
     return ring_bytes > red_bytes ? ring_bytes : red_bytes;
+}
+
+Geo tail_geo(uint32_t N) {
+    Geo g;
+    g.N = N;
+    const uint32_t Q = N / 4;
+    uint32_t tpr = Q < 32 ? Q : 32;
+    while (tpr > 1 && Q % tpr) tpr--;
+    g.tpr = tpr;
+    g.rps = 256 / tpr;
+    return g;
+}
+
+uint32_t tail_max_rows(uint32_t N, int reps, bool lane_hg) {
+    // about 256 KiB of table rows per CTA and round, and at most 1024 rows (the scalar tables
+    // of phase two sit in shared memory)
+    const Geo g = tail_geo(N);
+    const uint64_t per_row = (uint64_t)4 * g.tpr * 4 * (lane_hg ? 2 * reps : reps);
+    uint64_t rows = (256ull << 10) / per_row;
+    if (rows > 1024) rows = 1024;
+    uint32_t p = 1;
+    while ((uint64_t)p * 2 <= rows) p *= 2;
+    return p;
+}
+
+cudaError_t launch_tail(bool lane_hg, const TailArgs& a, cudaStream_t s) {
+    if (a.reps < 1 || a.reps > 3 || a.kt < 1 || a.kt >= a.n || a.n - a.kt > kMboxRounds - 1)
+        return cudaErrorInvalidValue;
+    const uint32_t S0 = 1u << (a.n - a.kt + 1);
+    if (S0 > 1024 || a.g.tpr < 1 || a.g.tpr > 32 || a.g.rps < 1 || a.g.tpr * a.g.rps > 256 || a.g.N % (4 * a.g.tpr))
+        return cudaErrorInvalidValue;
+    const dim3 grid(1, a.g.N / (4 * a.g.tpr), 1);
+    const size_t smem = 4 * ((lane_hg ? 0 : 2 * 3 * (size_t)S0) + 12 * 256 + 3 * 12 * (size_t)a.g.tpr);
+    if (lane_hg)
+        k_tail<true><<<grid, 256, smem, s>>>(a);
+    else
+        k_tail<false><<<grid, 256, smem, s>>>(a);
+    return cudaGetLastError();
 }
 
 uint32_t launch_stage_words(uint32_t* dst, const uint32_t* const* srcs, uint32_t nsrc, uint64_t n, unsigned int* done,
@@ -1631,7 +1853,7 @@ cudaError_t launch_p2_round01(int reps, const uint32_t* v, const uint32_t* const
     g.tpr = one_copy_slice(N);
     g.rps = 256 / g.tpr;
     const uint32_t groups = N / g.tpr;
-    uint64_t need = (ngroups + g.rps - 1) / g.rps, cap = ctas / groups;
+    uint64_t need = (ngroups + (uint64_t)g.rps * kMinRowIters - 1) / ((uint64_t)g.rps * kMinRowIters), cap = ctas / groups;
     if (cap < 1) cap = 1;
     if (need < 1) need = 1;
     const dim3 grid((uint32_t)(need < cap ? need : cap), groups, 1);

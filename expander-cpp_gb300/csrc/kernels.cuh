@@ -48,6 +48,33 @@ struct RoundPtrs {
     uint32_t hr[2][3];
 };
 
+// Persistent tail of a sumcheck phase (k_tail): rounds kt .. n-1 in one launch, one CTA per
+// lane group.  Round k folds its source tables at the challenges of round k-1 into its
+// destination tables (round k reads B and writes A when k is odd, the other way round when
+// k is even), publishes the round's evaluations to evals_out and bumps `done` once per CTA;
+// the last round also publishes rows 0..1 of each repetition's folded f table to rows_out.
+// The challenges of round k-1 > kt-1 come from the host through the mailbox (host-mapped
+// words: [0] abort, [4 + 4k] tag of round k's challenges = tag_base + k, [5 + 4k + j] r_k[j]).
+// Each wait is bounded by wait_ns: when it expires the kernel sets *err and returns; a
+// nonzero abort word makes it return at once.
+constexpr uint32_t kMboxRounds = 40;
+constexpr uint32_t kMboxWords = 4 + 4 * kMboxRounds;
+struct TailArgs {
+    uint32_t *fA[3], *fB[3];  // per-copy f tables
+    uint32_t *hA[3], *hB[3];  // per-copy hg tables (phase one) or scalar s tables (phase two)
+    const uint32_t* vx;       // phase two: R x N claims the sums are multiplied by; null in phase one
+    uint32_t r_first[3];      // challenges of round kt - 1
+    uint32_t kt, n, reps;
+    uint32_t tag_base;
+    const uint32_t* mbox;
+    uint32_t* evals_out;      // R x 3 x N
+    uint32_t* rows_out;       // R x 2 x N
+    unsigned int* done;
+    unsigned int* err;
+    unsigned long long wait_ns;
+    Geo g;
+};
+
 struct LaunchShape {
     dim3 grid, block;
     size_t smem;
@@ -69,6 +96,7 @@ enum KernelId {
     K_CANONICAL,   // verifier
     K_P2_ROUND0,
     K_STAGE,  // small transfers between device and host-mapped memory
+    K_TAIL,   // a phase's last rounds in one persistent launch (k_tail)
     // BN254 kernels (bn254.cuh)
     K_BN_LOAD,
     K_BN_EVALUATE,
@@ -170,6 +198,11 @@ cudaError_t launch_s_build4(uint64_t I, uint64_t O, const uint32_t* my_off, cons
                             cudaStream_t s);
 cudaError_t launch_s_build(uint64_t I, uint64_t O, const uint32_t* my_off, const uint4* my_g, const uint32_t* eqc,
                            const uint32_t* eqrx, uint32_t* s_out, uint64_t s_stride, uint32_t reps, cudaStream_t s);
+// Rows of a tail round's source tables above which a phase keeps its per-round kernels
+// (the tail's CTA reads all its rows alone), and the tile of the tail kernel.
+uint32_t tail_max_rows(uint32_t N, int reps, bool lane_hg);
+Geo tail_geo(uint32_t N);
+cudaError_t launch_tail(bool lane_hg, const TailArgs& a, cudaStream_t s);
 cudaError_t launch_wsum(int reps, const uint32_t* vals, uint64_t rows, const uint32_t* eq, const Geo& g,
                         uint32_t block, uint32_t ctas, RedScratch red, uint32_t* out, cudaStream_t s);
 

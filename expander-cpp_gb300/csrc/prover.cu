@@ -255,6 +255,10 @@ struct Lane {
     char* map_d = nullptr;
     size_t map_cap = 0, map_extra = 0;
     uint32_t done_seen = 0;
+    // tail kernels: tags of their mailbox challenges (never reused within a lane) and the
+    // mapped word a tail kernel sets when one of its waits expires (null: no tail running)
+    uint32_t tail_tag = 0;
+    const volatile uint32_t* tail_err = nullptr;
     uint32_t* evals_h() const { return reinterpret_cast<uint32_t*>(map_h); }
     uint32_t* evals_d() const { return reinterpret_cast<uint32_t*>(map_d); }
     char* extra_h() const { return map_h + map_extra; }
@@ -295,6 +299,8 @@ struct Lane {
                 if (e != cudaSuccess && e != cudaErrorNotReady) ck(e, "round kernel");
                 if (e == cudaSuccess && (int32_t)(*done_h() - target) < 0)
                     fail(GKRGPU_ERR_STATE, "round kernel finished without publishing its results");
+                if (tail_err && *tail_err)
+                    fail(GKRGPU_ERR_TIMEOUT, "a device wait for a round challenge expired");
                 if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60))
                     fail(GKRGPU_ERR_TIMEOUT, "round results not published within 60 s");
                 std::this_thread::yield();
@@ -374,6 +380,8 @@ struct gkrgpu_ctx {
     int n_lanes = 1, host_workers = 4, running = 0, host_threads_set = 0;
     int fs_hash = kFsSha256;  // transcript hash of jobs submitted from now on
     bool stopping = false;
+    // the last rounds of a phase in one persistent launch (k_tail) when their tables are small
+    bool round_tail = true;
     // copies of gkrgpu_upload: their own stream, so queued and running proofs go on
     std::mutex xfer_m;
     cudaStream_t xfer = nullptr;
@@ -788,7 +796,77 @@ struct Prover {
         }
     }
     ~Prover() {
+        // a tail kernel still waiting for a challenge returns at once
+        if (tail_running) {
+            mbox_h()[0] = 1u;
+            std::atomic_thread_fence(std::memory_order_seq_cst);
+        }
+        c.tail_err = nullptr;
         if (block) cudaFreeAsync(block, c.stream);
+    }
+
+    // Rounds kt .. n-1 of a phase in one k_tail launch: after each round's evaluations the
+    // host appends them, derives the challenges and writes them to the mailbox, from which
+    // the kernel's next round reads them.  The last round's rows 0..1 come with its
+    // evaluations (vx / vy as in transcript_round).
+    void run_tail(Transcript& t, bool lane_hg, uint32_t kt, uint32_t n, uint32_t (*rch)[32], uint32_t* const* fA,
+                  uint32_t* const* fB, uint32_t* const* hA, uint32_t* const* hB, bool append_last, uint32_t* last_out,
+                  double bytes) {
+        TailArgs a;
+        memset(&a, 0, sizeof(a));
+        for (int j = 0; j < R; j++) {
+            a.fA[j] = fA[j];
+            a.fB[j] = fB[j];
+            a.hA[j] = hA[j];
+            a.hB[j] = hB[j];
+            a.r_first[j] = rch[j][kt - 1];
+        }
+        a.vx = lane_hg ? nullptr : ws.vx;
+        a.kt = kt;
+        a.n = n;
+        a.reps = (uint32_t)R;
+        a.tag_base = c.tail_tag;
+        c.tail_tag += kMboxRounds;
+        a.mbox = mapped(true, 12ull * N + 64);
+        a.evals_out = c.evals_d();
+        a.rows_out = mapped(true, 0);
+        a.done = c.done_d();
+        a.err = mapped(true, 12ull * N + 1);
+        a.wait_ns = 10ull * 1000 * 1000 * 1000;
+        a.g = tail_geo(N);
+        const uint32_t groups = N / (4 * a.g.tpr);
+        volatile uint32_t* mb = mbox_h();
+        mb[0] = 0u;
+        *err_h() = 0u;
+        std::atomic_thread_fence(std::memory_order_seq_cst);
+        c.launch(K_TAIL, bytes, [&] { return launch_tail(lane_hg, a, c.stream); });
+        tail_running = true;
+        c.tail_err = err_h();
+        for (uint32_t k = kt; k < n; k++) {
+            c.wait_done(groups);
+            const bool last = k + 1 == n;
+            transcript_round(t, rch, k, last, append_last, last_out);
+            if (!last) {
+                for (int j = 0; j < R; j++) mb[4 + 4 * k + 1 + j] = rch[j][k];
+                std::atomic_thread_fence(std::memory_order_release);
+                mb[4 + 4 * k] = a.tag_base + k;
+                std::atomic_thread_fence(std::memory_order_seq_cst);
+            }
+        }
+        tail_running = false;
+        c.tail_err = nullptr;
+    }
+    // First round of a phase's tail, n if the phase has none: the rounds whose source tables
+    // have at most tail_max_rows rows, from round `first` on.
+    uint32_t tail_start(uint32_t n, uint32_t first, bool lane_hg) const {
+        if (!X.round_tail || n < first + 1) return n;
+        const uint32_t mr = tail_max_rows(N, R, lane_hg);
+        uint32_t lg = 0;
+        while ((1u << (lg + 1)) <= mr) lg++;
+        // source rows of round k: 2^(n - k + 1) <= mr  <=>  k >= n + 1 - lg
+        const uint32_t k0 = n + 1 > lg ? n + 1 - lg : 0;
+        const uint32_t kt = std::max(first, k0);
+        return kt < n ? kt : n;
     }
 
     RedScratch red() const { return RedScratch{ws.acc, ws.ticket}; }
@@ -803,6 +881,10 @@ struct Prover {
     uint32_t* cv_h() const { return mapped(false, 6ull * N); }
     uint32_t* vx_h() const { return mapped(false, 9ull * N); }
     volatile uint32_t* flag_h() const { return mapped(false, 12ull * N); }
+    // tail kernels: error word and challenge mailbox
+    volatile uint32_t* err_h() const { return mapped(false, 12ull * N + 1); }
+    volatile uint32_t* mbox_h() const { return mapped(false, 12ull * N + 64); }
+    bool tail_running = false;
     // Moves nsrc tables of n words into dst with k_stage_words (launch accounting as stage_words);
     // returns the number of completion increments when `done` is given.
     uint32_t stage(uint32_t* dst, const uint32_t* const* srcs, uint32_t nsrc, uint64_t n, unsigned int* done) {
@@ -823,7 +905,7 @@ struct Prover {
         block = static_cast<char*>(p);
         ws.plan(block, C, N, R, own_input, sumcheck);
         ck(cudaMemsetAsync(block + ws.zero_off, 0, ws.zero_bytes, c.stream), "cudaMemsetAsync");
-        c.ensure_mapped(9ull * N * 4, 12ull * N * 4 + 64);
+        c.ensure_mapped(9ull * N * 4, (12ull * N + 64 + kMboxWords) * 4);
         c.resync_done();
     }
 
@@ -957,7 +1039,17 @@ struct Prover {
 
         const uint32_t* cur_f[3] = {v, v, v};
         const uint32_t* cur_h[3] = {nullptr, nullptr, nullptr};  // round 1 rebuilds hg
+        // the last rounds, on small tables, run in one persistent launch (from round 4 on:
+        // rounds 2 and 3 refold the input and recompute copy-independent hg rows)
+        const uint32_t kt1 = tail_start(n, 4, true);
         for (uint32_t k = 1; k < n; k++) {
+            if (k == kt1) {
+                double bytes = 0;
+                for (uint32_t kk = kt1; kk < n; kk++) bytes += rb * 3.0 * R * 4.0 * (double)(I >> (kk + 1));
+                c.tag = ((uint32_t)li << 16) | (1u << 8) | k;
+                run_tail(t, true, kt1, n, rx, ws.fA, ws.fB, ws.hgA, ws.hg0, true, vxh, bytes);
+                break;
+            }
             RoundPtrs p;
             memset(&p, 0, sizeof(p));
             for (int j = 0; j < R; j++) {
@@ -1087,7 +1179,24 @@ struct Prover {
             transcript_round(t, ry, 0, n == 1, false, vy.data());
         }
         for (int j = 0; j < R; j++) cur_f[j] = v;
+        // phase two's tail from round 3 on (round 2 refolds the layer input)
+        const uint32_t kt2 = refold ? tail_start(n, 3, false) : n;
         for (uint32_t k = k_first; k < n; k++) {
+            if (k == kt2) {
+                double bytes = 0;
+                for (uint32_t kk = kt2; kk < n; kk++) {
+                    const double S = 4.0 * (double)(I >> (kk + 1));
+                    bytes += rb * (R * S + R * S / 2) + 6.0 * R * S;
+                }
+                uint32_t *sA[3], *sB[3];
+                for (int j = 0; j < R; j++) {
+                    sA[j] = ws.sb[1] + j * sstride;
+                    sB[j] = ws.sb[0] + j * sstride;
+                }
+                c.tag = ((uint32_t)li << 16) | (2u << 8) | k;
+                run_tail(t, false, kt2, n, ry, ws.fA, ws.fB, sA, sB, false, vy.data(), bytes);
+                break;
+            }
             RoundPtrs p;
             memset(&p, 0, sizeof(p));
             const int src = (k - 1) & 1, dst = k & 1;
@@ -1830,6 +1939,72 @@ int gkrgpu_eval_multilinear(gkrgpu_ctx* ctx, const uint32_t* d_evals, uint32_t n
             c.sync();
             memcpy(out, c.h_cv.p, n_points * rowb);
             c.resolve_events();
+        });
+    });
+}
+
+int gkrgpu_set_round_tail(gkrgpu_ctx* ctx, int enabled) {
+    return guarded([&] {
+        check_ctx(ctx);
+        ctx->drain();
+        ctx->round_tail = enabled != 0;
+    });
+}
+
+int gkrgpu_check_device_wait(gkrgpu_ctx* ctx, uint32_t timeout_us, int* expired, int* rounds_published) {
+    return guarded([&] {
+        check_ctx(ctx);
+        if (!expired || !rounds_published) fail(GKRGPU_ERR_INVALID, "null output");
+        if (timeout_us < 1 || timeout_us > 10u * 1000 * 1000) fail(GKRGPU_ERR_INVALID, "timeout_us must be in [1, 10^7]");
+        on_idle_lane(ctx, [&](Lane& c) {
+            // a two-round tail over 8 x 4 tables whose second round's challenge is never written
+            const uint32_t N = 4, n = 3, kt = 1;
+            const size_t tb = 8 * N * 4;
+            void* p = nullptr;
+            ck(cudaMallocFromPoolAsync(&p, 4 * tb, ctx->pool, c.stream), "workspace allocation");
+            struct Free {
+                void* p;
+                cudaStream_t s;
+                ~Free() {
+                    cudaFreeAsync(p, s);
+                    cudaStreamSynchronize(s);
+                }
+            } guard{p, c.stream};
+            ck(cudaMemsetAsync(p, 0, 4 * tb, c.stream), "cudaMemsetAsync");
+            c.ensure_mapped(9ull * N * 4, (12ull * N + 64 + kMboxWords) * 4);
+            c.resync_done();
+            uint32_t* base_h = reinterpret_cast<uint32_t*>(c.extra_h());
+            uint32_t* base_d = reinterpret_cast<uint32_t*>(c.extra_d());
+            TailArgs a;
+            memset(&a, 0, sizeof(a));
+            char* b = static_cast<char*>(p);
+            a.fA[0] = reinterpret_cast<uint32_t*>(b);
+            a.fB[0] = reinterpret_cast<uint32_t*>(b + tb);
+            a.hA[0] = reinterpret_cast<uint32_t*>(b + 2 * tb);
+            a.hB[0] = reinterpret_cast<uint32_t*>(b + 3 * tb);
+            a.kt = kt;
+            a.n = n;
+            a.reps = 1;
+            a.tag_base = c.tail_tag;
+            c.tail_tag += kMboxRounds;
+            a.mbox = base_d + 12 * N + 64;
+            a.evals_out = c.evals_d();
+            a.rows_out = base_d;
+            a.done = c.done_d();
+            a.err = base_d + 12 * N + 1;
+            a.wait_ns = (unsigned long long)timeout_us * 1000;
+            a.g = tail_geo(N);
+            volatile uint32_t* mb = base_h + 12 * N + 64;
+            volatile uint32_t* err = base_h + 12 * N + 1;
+            mb[0] = 0u;
+            *err = 0u;
+            std::atomic_thread_fence(std::memory_order_seq_cst);
+            ck(launch_tail(true, a, c.stream), "round_tail");
+            ck(cudaStreamSynchronize(c.stream), "round_tail");  // returns once the wait expires
+            std::atomic_thread_fence(std::memory_order_acquire);
+            *expired = *err ? 1 : 0;
+            *rounds_published = (int)(*c.done_h() - c.done_seen);
+            c.resync_done();
         });
     });
 }

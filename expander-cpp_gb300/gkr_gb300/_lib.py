@@ -83,6 +83,8 @@ SIGNATURES = [
     ("gkrgpu_memory_stats", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     ("gkrgpu_eval_multilinear", _I, [_P, _P, _U32, _U32, _P, _I, _P]),
     ("gkrgpu_eval_multilinear_noalloc", _I, [_P, _U32, _U32, _P, _I, _P, _P]),
+    ("gkrgpu_set_round_tail", _I, [_P, _I]),
+    ("gkrgpu_check_device_wait", _I, [_P, _U32, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("gkrgpu_device_alloc", _I, [_P, _U64, ctypes.POINTER(_P)]),
     ("gkrgpu_device_free", _I, [_P, _P]),
     ("gkrgpu_host_alloc", _I, [_U64, ctypes.POINTER(_P)]),

@@ -229,6 +229,17 @@ class Context:
         a = np.ascontiguousarray(host_array)
         _lib.check(_lib.load().gkrgpu_upload(self.handle, ctypes.c_void_p(d_dst), a.ctypes.data, a.nbytes))
 
+    def set_round_tail(self, enabled: bool):
+        """Phase tails in one persistent launch (default) or one launch per round."""
+        _lib.check(_lib.load().gkrgpu_set_round_tail(self.handle, int(enabled)))
+
+    def check_device_wait(self, timeout_us: int):
+        """gkrgpu_check_device_wait: (expired, rounds_published) of a tail whose second
+        challenge never comes."""
+        e, r = ctypes.c_int(), ctypes.c_int()
+        _lib.check(_lib.load().gkrgpu_check_device_wait(self.handle, timeout_us, ctypes.byref(e), ctypes.byref(r)))
+        return bool(e.value), r.value
+
     def set_host_threads(self, threads=0):
         """Host threads for host stages (commitment hashing); 0 restores the default."""
         _lib.check(_lib.load().gkrgpu_set_host_threads(self.handle, threads))

@@ -257,6 +257,19 @@ int gkrgpu_eval_multilinear(gkrgpu_ctx* ctx, const uint32_t* d_evals, uint32_t n
 int gkrgpu_eval_multilinear_noalloc(const uint32_t* d_evals, uint32_t nb_vars, uint32_t n_copies,
                                     const uint32_t* r, int n_points, uint32_t* d_out, void* stream);
 
+/* Persistent phase tails.  When the tables of a phase's last rounds are small, those rounds
+ * run in one launch (k_tail) that waits on the device for each round's challenges, which
+ * the host writes into host-mapped memory after hashing the round's evaluations, instead of
+ * one kernel launch per round.  On by default; gkrgpu_set_round_tail(ctx, 0) runs every
+ * round as its own launch (the proof bytes are the same).  No counterpart in the reference,
+ * whose sumcheck runs on the CPU (sumcheck.hpp:72-97). */
+int gkrgpu_set_round_tail(gkrgpu_ctx* ctx, int enabled);
+/* Checks the bounded device wait of the phase tails: runs a two-round tail whose second
+ * challenge is never written, with a wait limit of timeout_us, and reports whether the wait
+ * expired and the kernel returned (expired = 1) and how many rounds it published (1).  The
+ * context stays usable.  A diagnostic with no counterpart in the reference. */
+int gkrgpu_check_device_wait(gkrgpu_ctx* ctx, uint32_t timeout_us, int* expired, int* rounds_published);
+
 /* Device / pinned host buffers for callers without a CUDA allocator of their own. */
 int gkrgpu_device_alloc(gkrgpu_ctx* ctx, uint64_t bytes, void** out);
 int gkrgpu_device_free(gkrgpu_ctx* ctx, void* p);
