@@ -1668,6 +1668,11 @@ int gkrgpu_create(int device, gkrgpu_ctx** out) {
         ck(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
         if (const char* tp = getenv("GKRGPU_TRACE"))
             if (*tp) c->trace = fopen(tp, "a");
+        // Under a CUDA injection tool (a profiler) kernels may run one at a time with the
+        // launching thread blocked until each finishes; a phase tail, which waits on the device
+        // for its own host thread's challenges, would then only end at its wait limit.
+        if (const char* inj = getenv("CUDA_INJECTION64_PATH"))
+            if (*inj) c->round_tail = false;
         c->lane(0);
         if (c->trace) {
             ck(cudaEventCreate(&c->epoch), "cudaEventCreate");

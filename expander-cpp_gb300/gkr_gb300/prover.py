@@ -327,11 +327,21 @@ class Context:
 
 
 class Job:
-    """A queued proof (gkrgpu_job); keeps its buffers alive until waited on."""
+    """A queued proof (gkrgpu_job); keeps its buffers alive until waited on.  A job dropped
+    without Context.wait is waited for here, so its buffers are never freed while the library
+    still copies into them."""
 
     def __init__(self, handle, buffers):
         self.handle = handle
         self.buffers = buffers
+
+    def __del__(self):
+        h, self.handle = getattr(self, "handle", None), None
+        if h:
+            try:
+                _lib.load().gkrgpu_prove_wait(h, ctypes.byref(ctypes.c_uint64()))
+            except Exception:
+                pass
 
 
 class HostBuffer:

@@ -261,8 +261,11 @@ int gkrgpu_eval_multilinear_noalloc(const uint32_t* d_evals, uint32_t nb_vars, u
  * run in one launch (k_tail) that waits on the device for each round's challenges, which
  * the host writes into host-mapped memory after hashing the round's evaluations, instead of
  * one kernel launch per round.  On by default; gkrgpu_set_round_tail(ctx, 0) runs every
- * round as its own launch (the proof bytes are the same).  No counterpart in the reference,
- * whose sumcheck runs on the CPU (sumcheck.hpp:72-97). */
+ * round as its own launch (the proof bytes are the same).  A context created under a CUDA
+ * injection tool (CUDA_INJECTION64_PATH set, as profilers do) starts with the tails off:
+ * such tools may run each kernel to completion before the launching thread goes on, and a
+ * tail waits for that thread.  No counterpart in the reference, whose sumcheck runs on the
+ * CPU (sumcheck.hpp:72-97). */
 int gkrgpu_set_round_tail(gkrgpu_ctx* ctx, int enabled);
 /* Checks the bounded device wait of the phase tails: runs a two-round tail whose second
  * challenge is never written, with a wait limit of timeout_us, and reports whether the wait

@@ -83,3 +83,18 @@ def test_in_order_region_and_depth_bound():
 def test_timed_proofs_fit_the_marker_slots():
     with pytest.raises(ValueError):
         bench.pipelined(FakeCtx([0.0] * 70, [1.0] * 70), 1, bench.MAX_TIMED + 1, [None], lambda b, m: 0)
+
+
+def test_a_failed_proof_drains_the_others_before_unwinding():
+    class Failing(FakeCtx):
+        def wait(self, job):
+            super().wait(job)
+            if job == 2:
+                raise RuntimeError("proof 2 failed")
+
+    ctx = Failing([0.0] * 8, [float(i + 1) for i in range(8)])
+    with pytest.raises(RuntimeError):
+        bench.pipelined(ctx, 2, 6, [None] * 4, lambda b, m: ctx.submit(b, m))
+    # proofs 0..5 were submitted (depth 4 after two waits); every one of them was waited for
+    assert sorted(ctx.waited) == list(range(ctx.next_id))
+    assert ctx.in_flight == 0
