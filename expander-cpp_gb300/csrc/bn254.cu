@@ -416,7 +416,7 @@ __global__ void k_load(const uint32_t* __restrict__ canon, uint32_t* __restrict_
         uint32_t d[8];
         if (bad) {
             if (minus_r(x.l, d) == 0u) {  // no borrow: x >= r
-                atomicOr(bad, 1u);
+                *reinterpret_cast<volatile unsigned int*>(bad) = 1u;  // every writer stores 1 (device or mapped flag)
                 x = zero();
             }
         } else {

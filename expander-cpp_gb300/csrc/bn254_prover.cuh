@@ -95,6 +95,23 @@ struct BnProver {
     bn::RedBn red() const { return bn::RedBn{ws.acc, ws.ticket}; }
     bn::RedBn red_mapped() const { return bn::RedBn{ws.acc, ws.ticket, c.done_d()}; }
     uint32_t groups(int kid) const { return N / gk[kid].tpr; }
+    // The lane's mapped extra area (words): rows 0..1 of the last table (16N), the claims (8N),
+    // vx in Montgomery form (8N), the input check flag.  Small transfers go through it by
+    // kernels, never queueing on the copy engine behind another proof's bulk copies.
+    uint32_t* mapped(bool dev, uint64_t word) const {
+        return reinterpret_cast<uint32_t*>(dev ? c.extra_d() : c.extra_h()) + word;
+    }
+    volatile uint32_t* flag_h() const { return mapped(false, 32ull * N); }
+    uint32_t stage(uint32_t* dst, const uint32_t* src, uint64_t words, unsigned int* done) {
+        uint32_t incs = 0;
+        const uint32_t* srcs[1] = {src};
+        c.launch(K_STAGE, 8.0 * words, [&] {
+            cudaError_t e;
+            incs = launch_stage_words(dst, srcs, 1, words, done, c.stream, &e);
+            return e;
+        });
+        return done ? incs : 0;
+    }
 
     void reserve(bool sumcheck) {
         ws.plan(nullptr, C, N, sumcheck);
@@ -103,12 +120,8 @@ struct BnProver {
         block = static_cast<char*>(p);
         ws.plan(block, C, N, sumcheck);
         ck(cudaMemsetAsync(block + ws.zero_off, 0, ws.zero_bytes, c.stream), "cudaMemsetAsync");
-        c.ensure_mapped(3 * rowb());
+        c.ensure_mapped(3 * rowb(), (32ull * N + 64) * 4);
         c.resync_done();
-        c.h_rows.ensure(2 * rowb(), "pinned rows");
-        c.h_vx.ensure(rowb(), "pinned vx");
-        c.h_cv.ensure(rowb(), "pinned claims");
-        c.h_flag.ensure(4, "pinned flag");
     }
 
     void layout_values() {
@@ -130,11 +143,13 @@ struct BnProver {
             c.copy(ws.stage, h_input, n * 32, cudaMemcpyHostToDevice, "input upload");
             src = ws.stage;
         }
-        c.launch(K_BN_LOAD, 64.0 * n, [&] { return bn::launch_load(src, vals[0], n, ws.flag, c.stream); });
-        c.copy(c.h_flag.p, ws.flag, 4, cudaMemcpyDeviceToHost, "input check readback");
+        *flag_h() = 0u;
+        std::atomic_thread_fence(std::memory_order_seq_cst);
+        c.launch(K_BN_LOAD, 64.0 * n,
+                 [&] { return bn::launch_load(src, vals[0], n, mapped(true, 32ull * N), c.stream); });
     }
     void require_canonical() {
-        if (*c.h_flag.as<unsigned>()) fail(GKRGPU_ERR_INVALID, "input contains a value >= r (the BN254 modulus)");
+        if (*flag_h()) fail(GKRGPU_ERR_INVALID, "input contains a value >= r (the BN254 modulus)");
     }
 
     void evaluate() {
@@ -151,9 +166,8 @@ struct BnProver {
 
     // Waits for the round's 3 evaluation rows; optionally copies rows 0..1 of `rows_from`.
     void fetch(uint32_t groups, const uint32_t* rows_from) {
-        if (rows_from) c.copy(c.h_rows.p, rows_from, 2 * rowb(), cudaMemcpyDeviceToHost, "fetch rows");
-        c.wait_done(groups);
-        if (rows_from) c.sync();
+        const uint32_t more = rows_from ? stage(mapped(true, 0), rows_from, 16ull * N, c.done_d()) : 0u;
+        c.wait_done(groups + more);
     }
 
     // One round's transcript step (sumcheck.hpp:74-96 with R = 1): append the 3 rows, take
@@ -165,7 +179,7 @@ struct BnProver {
         rch[k] = t.challenge_bn254();
         if (!last) return;
         const frh::Fr rm = frh::to_mont(rch[k]);
-        const uint32_t* f0 = c.h_rows.as<uint32_t>();
+        const uint32_t* f0 = mapped(false, 0);
         const uint32_t* f1 = f0 + (size_t)N * 8;
         for (uint32_t i = 0; i < N; i++) {
             const frh::Fr m = frh::fold_mont(frh::load(f0 + 8 * i), frh::load(f1 + 8 * i), rm);
@@ -197,7 +211,7 @@ struct BnProver {
         const uint64_t I = 1ull << n;
         const double rb = (double)rowb();
         uint32_t* v = vals[li];
-        uint32_t* vx_m = c.h_vx.as<uint32_t>();
+        uint32_t* vx_m = mapped(false, 24ull * N);
         std::vector<uint32_t> vx_c((size_t)N * 8), vy_m((size_t)N * 8), vy_c((size_t)N * 8);
 
         // phase one: eqc = alpha eq(rz1) + beta eq(rz2), gate weights, hg + round 0
@@ -241,7 +255,7 @@ struct BnProver {
         c.launch(K_BN_S_BUILD, 16.0 * Ly.nmul + 4.0 * I + 32.0 * I + 96.0 * Ly.nmul, [&] {
             return bn::launch_s_build(I, Ly.my_off, Ly.my_g, Ly.my_c, ws.eqc, ws.eqrx, ws.sb[0], c.stream);
         });
-        c.copy(ws.vx, vx_m, rowb(), cudaMemcpyHostToDevice, "vx upload");
+        stage(ws.vx, mapped(true, 24ull * N), 8ull * N, nullptr);
         {
             bn::RoundPtrsBn p;
             memset(&p, 0, sizeof(p));
@@ -297,12 +311,12 @@ struct BnProver {
         eq_table(ws.eqc, rz1, nullptr, alpha, beta, nz);
         const uint64_t OL = C.out_rows(L - 1);
         c.launch(K_BN_WSUM, 32.0 * N * OL + 32.0 * OL, [&] {
-            return bn::launch_wsum(vals[L], OL, ws.eqc, gk[K_BN_WSUM], ctas[K_BN_WSUM], red(), ws.cv, c.stream);
+            return bn::launch_wsum(vals[L], OL, ws.eqc, gk[K_BN_WSUM], ctas[K_BN_WSUM], red(), mapped(true, 16ull * N),
+                                   c.stream);
         });
-        c.copy(c.h_cv.p, ws.cv, rowb(), cudaMemcpyDeviceToHost, "claims readback");
         c.sync();
         require_canonical();
-        memcpy(claimed_v, c.h_cv.p, rowb());
+        memcpy(claimed_v, mapped(false, 16ull * N), rowb());
 
         for (int li = (int)L - 1; li >= 0; li--) {
             sumcheck_layer(t, (size_t)li, rz1, have_rz2 ? rz2 : nullptr, alpha, beta, rx, ry);
