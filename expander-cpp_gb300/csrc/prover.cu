@@ -226,6 +226,7 @@ struct gkrgpu_job {
 
 // ------------------------------------------------------------------ lanes
 // One device worker's state: its stream, pinned staging buffers, launch accounting.
+constexpr size_t kMinMapped = 2u << 20;  // mapped staging per lane: enough for 16384 copies of M31
 struct Lane {
     gkrgpu_ctx* X = nullptr;
     cudaStream_t stream = nullptr;
@@ -269,7 +270,10 @@ struct Lane {
     void ensure_mapped(size_t evals_bytes, size_t extra_bytes = 0) {
         const size_t ev = align_up(evals_bytes, 256), ex = align_up(extra_bytes, 256);
         if (map_h && ev <= map_extra && map_extra + ex + 256 <= map_cap) return;
-        const size_t ev_new = std::max(ev, map_extra), ex_new = std::max(ex, map_h ? map_cap - 256 - map_extra : 0);
+        // at least kMinMapped bytes at once: freeing a pinned block synchronizes the whole device,
+        // so a lane should not grow it proof by proof
+        const size_t ev_new = std::max({ev, map_extra, kMinMapped / 4}),
+                     ex_new = std::max({ex, map_h ? map_cap - 256 - map_extra : 0, kMinMapped - kMinMapped / 4});
         const size_t need = ev_new + ex_new + 256;
         if (map_h) cudaFreeHost(map_h);
         map_h = map_d = nullptr;
