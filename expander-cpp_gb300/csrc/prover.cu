@@ -37,6 +37,9 @@
 #include <string>
 #include <thread>
 #include <vector>
+#ifdef __linux__
+#include <sys/prctl.h>
+#endif
 
 #include "../../include/gkrgpu.h"
 #include "bn254.cuh"
@@ -256,6 +259,10 @@ struct Lane {
     char* map_d = nullptr;
     size_t map_cap = 0, map_extra = 0;
     uint32_t done_seen = 0;
+    // algorithmic bytes launched since the last wait, and when the first of them was launched
+    double pending_bytes = 0;
+    int X_lanes = 1;  // the context's lane count when this lane's worker started
+    std::chrono::steady_clock::time_point pending_t0;
     // tail kernels: tags of their mailbox challenges (never reused within a lane) and the
     // mapped word a tail kernel sets when one of its waits expires (null: no tail running)
     uint32_t tail_tag = 0;
@@ -295,10 +302,23 @@ struct Lane {
     // went idle or failed without them is an error; the wait is bounded.
     void wait_done(uint32_t groups) {
         const uint32_t target = done_seen + groups;
+        // Sleep through most of the expected run time of what was launched since the last
+        // wait (its algorithmic bytes at about the copy peak, woken early), then spin: a lane
+        // thread spinning through a long kernel takes a core from the host stages' hashing.
+        if (pending_bytes > 0 && (int32_t)(*done_h() - target) < 0) {
+            const auto wake = pending_t0 + std::chrono::nanoseconds((int64_t)(pending_bytes / 7.5e3));
+            if (wake - std::chrono::steady_clock::now() > std::chrono::microseconds(30))
+                std::this_thread::sleep_until(wake);
+        }
+        pending_bytes = 0;
         const auto t0 = std::chrono::steady_clock::now();
+        // With several lanes the host cores are shared with the host stages' hashing: after a
+        // short spin, poll in 10 us sleeps instead of spinning.
+        const bool share_cores = X_lanes >= 4;
         for (uint64_t it = 0;; it++) {
             if ((int32_t)(*done_h() - target) >= 0) break;
-            if ((it & 1023) == 1023) {
+            if (share_cores && it >= 2048) std::this_thread::sleep_for(std::chrono::microseconds(10));
+            if ((it & 1023) == 1023 || (share_cores && it >= 2048)) {
                 const cudaError_t e = cudaStreamQuery(stream);
                 if (e != cudaSuccess && e != cudaErrorNotReady) ck(e, "round kernel");
                 if (e == cudaSuccess && (int32_t)(*done_h() - target) < 0)
@@ -488,6 +508,8 @@ struct gkrgpu_ctx {
 
 template <class F>
 void Lane::launch(int kid, double algo_bytes, F&& f) {
+    if (pending_bytes == 0) pending_t0 = std::chrono::steady_clock::now();
+    pending_bytes += algo_bytes;
     size_t e0 = 0;
     if (X->timing) {
         e0 = next_event();
@@ -844,6 +866,7 @@ struct Prover {
         *err_h() = 0u;
         std::atomic_thread_fence(std::memory_order_seq_cst);
         c.launch(K_TAIL, bytes, [&] { return launch_tail(lane_hg, a, c.stream); });
+        c.pending_bytes = 0;  // its rounds are short and each waits for the host: no sleeping
         tail_running = true;
         c.tail_err = err_h();
         for (uint32_t k = kt; k < n; k++) {
@@ -1461,6 +1484,11 @@ void host_worker(gkrgpu_ctx* c) {
 
 void gpu_worker(gkrgpu_ctx* c, Lane* lane) {
     cudaSetDevice(c->device);
+    lane->X_lanes = c->n_lanes;
+#ifdef __linux__
+    // wake from the sleeps of Lane::wait_done within a microsecond of the requested time
+    prctl(PR_SET_TIMERSLACK, 1000UL, 0, 0, 0);
+#endif
     for (;;) {
         gkrgpu_job* j;
         {

@@ -40,7 +40,9 @@ def test_tails_in_concurrent_lanes(oracle):
     c = Context(0)
     try:
         c.set_concurrency(lanes=4)
+        # proofs of 2^8 .. 2^14-row layers in four lanes at once, each with its own tails
         specs = [(511 + i, [8 + i % 3, 9, 8 + i % 2], 16 * (1 + i % 4)) for i in range(8)]
+        specs += [(531, [13, 12, 13], 16), (532, [14, 13], 32), (533, [12, 14, 12], 64), (534, [14, 11, 14], 16)]
         circs = [gc.random_circuit(s, wd) for s, wd, _ in specs]
         wits = [gc.random_witness(s, cc.log_input_size, n) for (s, _, n), cc in zip(specs, circs)]
         dcs = [c.load(cc) for cc in circs]
