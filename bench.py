@@ -713,6 +713,7 @@ def serve_rate(srv, dcs, wits, rate, duration, seed):
         try:
             res = f.result()
             lats.append(res.latency_ms)
+            res.release()
             t_last = max(t_last, time.perf_counter())
         except Rejected:
             rejected += 1

@@ -15,6 +15,10 @@ admitted in two steps, both by footprint:
 Up to `lanes` proofs run their device stages at once and whatever is pending is taken into
 the lanes as earlier proofs finish, whatever its size.  Requests beyond `max_queue` waiting
 for admission are rejected (admission control), and every result carries its latency.
+Proof buffers come from a pool the server keeps per size: a caller done with a result hands
+its buffer back with Result.release(), so a steady stream of requests writes its proofs into
+memory that is already mapped (a fresh multi-megabyte buffer per request pays first-touch
+page faults, which stall for long when the host is reclaiming or compacting memory).
 
 The reference has no serving loop (benchmarks/bench_keccak.cpp:32-42 proves in a closed
 loop, one proof per thread).
@@ -75,11 +79,19 @@ class Arena:
 class Result:
     """A finished request: claimed values (R, N), the proof bytes (uint8 array) and times."""
 
-    def __init__(self, claimed_v, proof, latency_ms, admit_wait_ms):
+    def __init__(self, claimed_v, proof, latency_ms, admit_wait_ms, server=None, buf=None):
         self.claimed_v = claimed_v
         self.proof = proof
         self.latency_ms = latency_ms
         self.admit_wait_ms = admit_wait_ms
+        self._server, self._buf = server, buf
+
+    def release(self):
+        """Hands the proof buffer back to the server for later requests; `proof` must not be
+        used afterwards."""
+        if self._server is not None and self._buf is not None:
+            self._server._give_back(self._buf)
+        self.proof, self._server, self._buf = None, None, None
 
 
 class _Req:
@@ -105,7 +117,7 @@ class ProofServer:
     caps the requests in flight."""
 
     def __init__(self, ctx, lanes=16, budget_bytes=150 << 30, arena_bytes=16 << 30, max_queue=1 << 20,
-                 max_admitted=None):
+                 max_admitted=None, pool_bytes=8 << 30):
         self.ctx = ctx
         self.lanes = lanes
         self.budget = budget_bytes
@@ -123,6 +135,8 @@ class ProofServer:
         self.rejected = 0
         self.completed = 0
         self.stopping = False
+        self.pool = {}  # proof buffers handed back, by size, up to pool_bytes in all
+        self.pool_bytes, self.pooled = pool_bytes, 0
         self.threads = [threading.Thread(target=self._admit_loop, daemon=True)]
         self.threads += [threading.Thread(target=self._wait_loop, daemon=True) for _ in range(lanes)]
         for t in self.threads:
@@ -169,6 +183,21 @@ class ProofServer:
                     "witness_peak_bytes": self.peak, "arena_bytes": self.arena.size,
                     "workspace_peak_bytes": mem["peak"], "budget_bytes": self.budget}
 
+    # ---------------------------------------------------------------- proof buffers
+    def _take(self, size):
+        with self.cv:
+            free = self.pool.get(size)
+            if free:
+                self.pooled -= size
+                return free.pop()
+        return np.empty(size, np.uint8)
+
+    def _give_back(self, buf):
+        with self.cv:
+            if self.pooled + buf.size <= self.pool_bytes:
+                self.pool.setdefault(buf.size, []).append(buf)
+                self.pooled += buf.size
+
     # ---------------------------------------------------------------- threads
     def _fits(self):
         return self.max_admitted is None or self.in_flight < self.max_admitted
@@ -194,7 +223,7 @@ class ProofServer:
                 d_in = self.buf.ptr + r.off
                 w = r.witness
                 self.ctx.upload(d_in, w)
-                r.proof = np.empty(r.dc.proof_size(r.n, r.grinding_bits), np.uint8)
+                r.proof = self._take(r.dc.proof_size(r.n, r.grinding_bits))
                 r.claims = np.empty((r.dc.num_repetitions(r.grinding_bits),) + w.shape[1:], w.dtype)
                 r.job = self.ctx.submit_resident(r.dc, w, d_in, r.proof, r.claims, grinding_bits=r.grinding_bits)
             except Exception as e:  # noqa: BLE001 - the request fails, the loop goes on
@@ -230,4 +259,4 @@ class ProofServer:
             r.future.set_exception(error)
         else:
             r.future.set_result(Result(r.claims, r.proof[:length], (t - r.t_arr) * 1000.0,
-                                       ((r.t_adm or t) - r.t_arr) * 1000.0))
+                                       ((r.t_adm or t) - r.t_arr) * 1000.0, self, r.proof))

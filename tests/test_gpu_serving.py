@@ -52,6 +52,24 @@ def test_requests_in_the_mix_equal_the_proofs_made_alone(jobs):
     assert 0 < st["workspace_peak_bytes"] <= st["budget_bytes"]
 
 
+def test_released_proof_buffers_are_reused(jobs):
+    from gkr_gb300.serving import ProofServer
+    ctx, dcs, wits, alone = jobs
+    srv = ProofServer(ctx, lanes=2, budget_bytes=4 << 30, arena_bytes=256 << 20)
+    try:
+        first = srv.submit(dcs[2], wits[2]).result(timeout=60)
+        assert first.proof.tobytes() == alone[2][1]
+        buf = first._buf
+        first.release()
+        again = srv.submit(dcs[2], wits[2]).result(timeout=60)
+        assert again._buf is buf  # the same memory, rewritten
+        assert again.proof.tobytes() == alone[2][1]
+        other = srv.submit(dcs[5], wits[5]).result(timeout=60)  # another size: a buffer of its own
+        assert other.proof.tobytes() == alone[5][1]
+    finally:
+        srv.close()
+
+
 def test_request_on_an_idle_server(jobs):
     from gkr_gb300.serving import ProofServer
     ctx, dcs, wits, alone = jobs
