@@ -336,6 +336,22 @@ __global__ void k_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* _
     }
 }
 
+// w_j[k] (1 - r_j) for the mul gates of even input rows x, w_j[k] r_j for odd x: the weights
+// of k_hg_round1, whose sum over the gates of rows 2i and 2i+1 is then hg folded at r_j.
+__global__ void k_scale_weights(uint64_t I, const uint32_t* __restrict__ mx_off, const uint4* __restrict__ w4,
+                                uint4* __restrict__ w4r, uint4 r) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < I; x += stride) {
+        const bool odd = x & 1;
+        const uint32_t s0 = odd ? r.x : sub(1u, r.x), s1 = odd ? r.y : sub(1u, r.y), s2 = odd ? r.z : sub(1u, r.z);
+        const uint32_t k0 = __ldg(mx_off + x), k1 = __ldg(mx_off + x + 1);
+        for (uint32_t k = k0; k < k1; k++) {
+            const uint4 w = __ldg(w4 + k);
+            w4r[k] = make_uint4(mul(w.x, s0), mul(w.y, s1), mul(w.z, s2), 0u);
+        }
+    }
+}
+
 // ---------------------------------------------------------------- finishers
 // Evaluations at 0, 1, 2 of every repetition's round polynomial for one lane; with vx the
 // phase-two sums are multiplied by v(rx) (h = v(rx) * s).
@@ -344,13 +360,10 @@ struct RoundFin {
     uint32_t* out;       // R x 3 x N
     const uint32_t* vx;  // R x N, or null
     uint32_t N, reps;
-    bool cross = false;  // component 2 holds sum f0 h1 + f1 h0 instead of p2raw
     __device__ void operator()(uint32_t lane) const {
         for (uint32_t j = 0; j < reps; j++) {
             uint32_t p0 = take(red, 3 * j, N, lane), p1 = take(red, 3 * j + 1, N, lane);
-            uint32_t c2 = take(red, 3 * j + 2, N, lane);
-            if (cross) c2 = add(add(p0, p1), c2);
-            uint32_t p2 = m31::eval_at_two(p0, p1, c2);
+            uint32_t p2 = m31::eval_at_two(p0, p1, take(red, 3 * j + 2, N, lane));
             if (vx) {
                 const uint32_t x = vx[(size_t)j * N + lane];
                 p0 = mul(p0, x); p1 = mul(p1, x); p2 = mul(p2, x);
@@ -358,6 +371,39 @@ struct RoundFin {
             out[(size_t)(3 * j) * N + lane] = p0;
             out[(size_t)(3 * j + 1) * N + lane] = p1;
             out[(size_t)(3 * j + 2) * N + lane] = p2;
+        }
+    }
+};
+
+// Round evaluations from two sums per repetition, p0 and p2raw: p1 is the round's claim less
+// p0 (an honest prover's round polynomial meets p0 + p1 = claim, the verifier's check in
+// sumcheck.hpp:152, so p1 is the same field element as its direct sum).  The claim is
+// `claim` (R x N, written by the host before the launch), or with `prev` the previous
+// round's polynomial at its challenge r_j, eval_degree2 of its three evaluations: `prev` is
+// the buffer this finisher overwrites, each lane read before it is written.
+struct ClaimFin {
+    RedScratch red;
+    uint32_t* out;            // R x 3 x N
+    const uint32_t* claim;    // R x N, or null
+    const uint32_t* prev;     // R x 3 x N, or null
+    uint32_t r[3];
+    uint32_t N, reps;
+    __device__ void operator()(uint32_t lane) const {
+        for (uint32_t j = 0; j < reps; j++) {
+            uint32_t cl;
+            if (prev) {
+                const uint32_t rj = j == 0 ? r[0] : (j == 1 ? r[1] : r[2]);
+                cl = m31::eval_degree2(__ldcv(prev + (size_t)(3 * j) * N + lane),
+                                       __ldcv(prev + (size_t)(3 * j + 1) * N + lane),
+                                       __ldcv(prev + (size_t)(3 * j + 2) * N + lane), rj);
+            } else {
+                cl = __ldcv(claim + (size_t)j * N + lane);
+            }
+            const uint32_t p0 = take(red, 2 * j, N, lane), p2raw = take(red, 2 * j + 1, N, lane);
+            const uint32_t p1 = sub(cl, p0);
+            out[(size_t)(3 * j) * N + lane] = p0;
+            out[(size_t)(3 * j + 1) * N + lane] = p1;
+            out[(size_t)(3 * j + 2) * N + lane] = m31::eval_at_two(p0, p1, p2raw);
         }
     }
 };
@@ -412,13 +458,12 @@ __device__ __forceinline__ void cp_async_wait() {
 // (k_hg_round1) rebuilds it, which costs the gathers again but saves writing and re-reading
 // R full-width tables.  All repetitions in one thread: each gathered v[y] row serves the R
 // weights.
-// The round reads 4 bytes per copy and row and is bound by the integer multiply pipe, so
-// the sums p0 = sum f0 h0, p1 = sum f1 h1 and p2raw = sum (f0 + f1)(h0 + h1) take each product
-// unreduced below 2^32 (mac_lazy) with h of one row live at a time: a row adds f_s h to p_s
-// and (f0 + f1) h to p2raw.  A pair whose rows both lack mul gates (most pairs of a wide
-// layer) has the scalar add weights as h and costs three products per copy and repetition:
-// f0 a0, f1 a1 and (f0 + f1)(a0 + a1).  The pair's two input rows, their add-gate weights and
-// CSR offsets are staged by cp.async kStages - 1 iterations ahead.
+// The round reads 4 bytes per copy and row and is bound by the integer multiply pipe, so it
+// sums only p0 = sum f0 h0 and p2raw = sum (f0 + f1)(h0 + h1), each product added unreduced
+// below 2^32 (mac_lazy); p1 is the layer's claim less p0 (ClaimFin).  A pair whose rows both
+// lack mul gates (most pairs of a wide layer) has the scalar add weights as h and costs two
+// products per copy and repetition: f0 a0 and (f0 + f1)(a0 + a1).  The pair's two input rows,
+// their add-gate weights and CSR offsets are staged by cp.async kStages - 1 iterations ahead.
 constexpr int kStages = 3;
 constexpr int kStageFields = 5;  // v(2i), v(2i+1), a(2i), a(2i+1), (off(2i), off(2i+1), off(2i+2))
 constexpr int kMaxStagedSmem = kStages * kStageFields * 16 * 256;
@@ -429,34 +474,18 @@ __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict
                                                       const uint32_t* __restrict__ mx_off,
                                                       const uint4* __restrict__ mx_g, const uint4* __restrict__ a4,
                                                       const uint4* __restrict__ w4, Geo g, RedScratch red,
-                                                      uint32_t* evals_out) {
+                                                      const uint32_t* claim, uint32_t* evals_out) {
     extern __shared__ uint4 ring[];  // kStages x kStageFields x blockDim.x
     const TileIdx t = tile_idx(g);
     const uint32_t B = blockDim.x, tid = threadIdx.x;
-    uint32_t acc[3 * R][4];
+    uint32_t acc[2 * R][4];  // 2j: p0, 2j + 1: p2raw
 #pragma unroll
-    for (int c = 0; c < 3 * R; c++)
+    for (int c = 0; c < 2 * R; c++)
 #pragma unroll
         for (int l = 0; l < 4; l++) acc[c][l] = 0u;
-    // row x of the pair (s = 0: x = 2i, s = 1: x = 2i+1): p_s += f_s h, p2raw += (f0 + f1) h
-    auto row = [&](int s, const uint4& fs, const uint4& fo, const uint4& a, uint32_t k0, uint32_t k1) {
-        if (k0 == k1) {
-#pragma unroll
-            for (int l = 0; l < 4; l++) {
-                const uint32_t f01 = add(comp(fs, l), comp(fo, l));
-#pragma unroll
-                for (int j = 0; j < R; j++) {
-                    acc[3 * j + s][l] = m31::mac_lazy(acc[3 * j + s][l], comp(fs, l), comp(a, j));
-                    acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], f01, comp(a, j));
-                }
-            }
-            return;
-        }
-        uint32_t h[R][4];
-#pragma unroll
-        for (int j = 0; j < R; j++)
-#pragma unroll
-            for (int l = 0; l < 4; l++) h[j][l] = comp(a, j);
+    // adds the mul-gate terms of input row x (gates k0 .. k1) to h, canonical before and after
+    auto gates = [&](uint32_t k0, uint32_t k1, uint32_t (&h)[R][4]) {
+        if (k0 == k1) return;
         for (uint32_t k = k0; k < k1; k++) {
             const uint32_t y = __ldg(&mx_g[k].x);
             const uint4 w = __ldg(w4 + k);
@@ -467,15 +496,9 @@ __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict
                 for (int l = 0; l < 4; l++) h[j][l] = m31::mac_lazy(h[j][l], comp(vy, l), comp(w, j));
         }
 #pragma unroll
-        for (int l = 0; l < 4; l++) {
-            const uint32_t f01 = add(comp(fs, l), comp(fo, l));
+        for (int j = 0; j < R; j++)
 #pragma unroll
-            for (int j = 0; j < R; j++) {
-                const uint32_t hc = m31::from_u32(h[j][l]);
-                acc[3 * j + s][l] = m31::mac_lazy(acc[3 * j + s][l], comp(fs, l), hc);
-                acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], f01, hc);
-            }
-        }
+            for (int l = 0; l < 4; l++) h[j][l] = m31::from_u32(h[j][l]);
     };
     if (t.active) {
         // iteration i works on pair q = group_at(pairs, i) (rows 2q, 2q+1); the list entry of
@@ -509,22 +532,42 @@ __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict
             cp_async_wait<kStages - 1>();
             const uint4* st = ring + (size_t)slot * kStageFields * B + tid;
             const uint4 f0 = st[0], f1 = st[B], off = st[4 * B];
+            uint32_t f01[4];
+#pragma unroll
+            for (int l = 0; l < 4; l++) f01[l] = add(comp(f0, l), comp(f1, l));
             if (off.x == off.z) {  // neither row has mul gates
 #pragma unroll
                 for (int j = 0; j < R; j++) {
                     const uint32_t a0 = reinterpret_cast<const uint32_t*>(st + 2 * B)[j];
-                    const uint32_t a1 = reinterpret_cast<const uint32_t*>(st + 3 * B)[j];
-                    const uint32_t a01 = add(a0, a1);
+                    const uint32_t a01 = add(a0, reinterpret_cast<const uint32_t*>(st + 3 * B)[j]);
 #pragma unroll
                     for (int l = 0; l < 4; l++) {
-                        acc[3 * j][l] = m31::mac_lazy(acc[3 * j][l], comp(f0, l), a0);
-                        acc[3 * j + 1][l] = m31::mac_lazy(acc[3 * j + 1][l], comp(f1, l), a1);
-                        acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], add(comp(f0, l), comp(f1, l)), a01);
+                        acc[2 * j][l] = m31::mac_lazy(acc[2 * j][l], comp(f0, l), a0);
+                        acc[2 * j + 1][l] = m31::mac_lazy(acc[2 * j + 1][l], f01[l], a01);
                     }
                 }
             } else {
-                row(0, f0, f1, st[2 * B], off.x, off.y);
-                row(1, f1, f0, st[3 * B], off.y, off.z);
+                // h = hg(2q), then hg(2q) + hg(2q+1): row 2q+1's add weights and gate terms are
+                // added onto row 2q's hg
+                uint32_t h[R][4];
+                const uint4 a0 = st[2 * B], a1 = st[3 * B];
+#pragma unroll
+                for (int j = 0; j < R; j++)
+#pragma unroll
+                    for (int l = 0; l < 4; l++) h[j][l] = comp(a0, j);
+                gates(off.x, off.y, h);
+#pragma unroll
+                for (int j = 0; j < R; j++)
+#pragma unroll
+                    for (int l = 0; l < 4; l++) {
+                        acc[2 * j][l] = m31::mac_lazy(acc[2 * j][l], comp(f0, l), h[j][l]);
+                        h[j][l] = add(h[j][l], comp(a1, j));
+                    }
+                gates(off.y, off.z, h);
+#pragma unroll
+                for (int j = 0; j < R; j++)
+#pragma unroll
+                    for (int l = 0; l < 4; l++) acc[2 * j + 1][l] = m31::mac_lazy(acc[2 * j + 1][l], f01[l], h[j][l]);
             }
             slot = slot + 1 == kStages ? 0 : slot + 1;
         }
@@ -532,29 +575,33 @@ __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict
     }
     __syncthreads();  // the ring is reused as the reduction's scratch (sums below 2^32 are
                       // added as they are: the finisher reduces the 64-bit totals)
-    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R});
+    reduce_group<2 * R>(acc, g, t.active, red, 0,
+                        ClaimFin{red, evals_out, claim, nullptr, {0u, 0u, 0u}, g.N, (uint32_t)R});
 }
 
 // ---------------------------------------------------------------- phase one, round 1
 // Round 1 with hg rebuilt rather than read: for each output pair i the four source rows
 // x = 4i..4i+3 get hg_j[x] = a_j[x] + sum over mul gates (x, y, k) of v[y] w_j[k] again,
+// already folded (the fold is linear: the gate weights come scaled by 1 - r_j for even x and
+// r_j for odd x, so one sum over both rows' gates is the folded hg),
 // and hg_j and the layer input are folded at r_j into rows 2i, 2i+1 of hdst_j / fdst_j
 // (what receive_challenge of round 0 would have left, sumcheck_helper.hpp:104-133), which
 // are stored and summed into the round-1 evaluations.  All repetitions in one thread, as in
 // k_hg_round0: each gathered v[y] row serves the R weights.  When neither source row of an
 // output row has mul gates, its hg is the same for every copy: fold(a_j[x0], a_j[x1], r_j)
-// is computed once.  The sums use the cross form of k_hg_round0 (p0, p1, pc with mac_lazy);
-// after the first row of a pair only its f and h are kept, for pc.
+// is computed once.  The sums are those of k_hg_round0, p0 and p2raw with mac_lazy (p1 is
+// the claim, round 0's polynomial at r_j, less p0); after the first row of a pair only its
+// f and h are kept, for p2raw.
 template <int R>
 __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ v, uint64_t npairs,
                                                    const uint32_t* __restrict__ quads,
                                                    const uint32_t* __restrict__ mx_off, const uint4* __restrict__ mx_g,
-                                                   const uint4* __restrict__ a4, const uint4* __restrict__ w4,
+                                                   const uint4* __restrict__ a4, const uint4* __restrict__ w4r,
                                                    RoundPtrs p, Geo g, RedScratch red, uint32_t* evals_out) {
     const TileIdx t = tile_idx(g);
-    uint32_t acc[3 * R][4];
+    uint32_t acc[2 * R][4];  // 2j: p0, 2j + 1: p2raw
 #pragma unroll
-    for (int c = 0; c < 3 * R; c++)
+    for (int c = 0; c < 2 * R; c++)
 #pragma unroll
         for (int l = 0; l < 4; l++) acc[c][l] = 0u;
     if (t.active) {
@@ -574,39 +621,30 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
                 const uint64_t x0 = 4 * i + 2 * s;
                 const uint4 v0 = ld4(v, x0, g.N, t.lane0), v1 = ld4(v, x0 + 1, g.N, t.lane0);
                 const uint4 a0 = __ldg(a4 + x0), a1 = __ldg(a4 + x0 + 1);
+                // fold(hg(x0), hg(x1), r_j) = fold(a_j(x0), a_j(x1), r_j) plus the gate terms of
+                // rows x0 and x1 (gates off(x0) .. off(x0 + 2), contiguous) with their weights
+                // scaled by 1 - r_j and r_j (w4r, k_scale_weights)
                 uint32_t h[R][4];
-                if (off[2 * s] == off[2 * s + 2]) {
 #pragma unroll
-                    for (int j = 0; j < R; j++) {
-                        const uint32_t hs = fold(comp(a0, j), comp(a1, j), p.r[j]);
+                for (int j = 0; j < R; j++) {
+                    const uint32_t hs = fold(comp(a0, j), comp(a1, j), p.r[j]);
 #pragma unroll
-                        for (int l = 0; l < 4; l++) h[j][l] = hs;
-                    }
-                } else {
-                    uint32_t hx[2][R][4];
-#pragma unroll
-                    for (int e = 0; e < 2; e++) {
-                        const uint4& a = e ? a1 : a0;
+                    for (int l = 0; l < 4; l++) h[j][l] = hs;
+                }
+                if (off[2 * s] != off[2 * s + 2]) {
+                    for (uint32_t k = off[2 * s]; k < off[2 * s + 2]; k++) {
+                        const uint32_t y = __ldg(&mx_g[k].x);
+                        const uint4 w = __ldg(w4r + k);
+                        const uint4 vy = ld4(v, y, g.N, t.lane0);
 #pragma unroll
                         for (int j = 0; j < R; j++)
 #pragma unroll
-                            for (int l = 0; l < 4; l++) hx[e][j][l] = comp(a, j);
-                        for (uint32_t k = off[2 * s + e]; k < off[2 * s + e + 1]; k++) {
-                            const uint32_t y = __ldg(&mx_g[k].x);
-                            const uint4 w = __ldg(w4 + k);
-                            const uint4 vy = ld4(v, y, g.N, t.lane0);
-#pragma unroll
-                            for (int j = 0; j < R; j++)
-#pragma unroll
-                                for (int l = 0; l < 4; l++)
-                                    hx[e][j][l] = m31::mac_lazy(hx[e][j][l], comp(vy, l), comp(w, j));
-                        }
+                            for (int l = 0; l < 4; l++) h[j][l] = m31::mac_lazy(h[j][l], comp(vy, l), comp(w, j));
                     }
 #pragma unroll
                     for (int j = 0; j < R; j++)
 #pragma unroll
-                        for (int l = 0; l < 4; l++)
-                            h[j][l] = fold(m31::from_u32(hx[0][j][l]), m31::from_u32(hx[1][j][l]), p.r[j]);
+                        for (int l = 0; l < 4; l++) h[j][l] = m31::from_u32(h[j][l]);
                 }
 #pragma unroll
                 for (int j = 0; j < R; j++) {
@@ -620,20 +658,20 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
 #pragma unroll
                     for (int l = 0; l < 4; l++) {
                         if (s == 0) {
-                            acc[3 * j][l] = m31::mac_lazy(acc[3 * j][l], f[l], h[j][l]);
+                            acc[2 * j][l] = m31::mac_lazy(acc[2 * j][l], f[l], h[j][l]);
                             fe[j][l] = f[l];
                             he[j][l] = h[j][l];
                         } else {
-                            acc[3 * j + 1][l] = m31::mac_lazy(acc[3 * j + 1][l], f[l], h[j][l]);
-                            acc[3 * j + 2][l] =
-                                m31::mac_lazy(m31::mac_lazy(acc[3 * j + 2][l], fe[j][l], h[j][l]), f[l], he[j][l]);
+                            acc[2 * j + 1][l] =
+                                m31::mac_lazy(acc[2 * j + 1][l], add(fe[j][l], f[l]), add(he[j][l], h[j][l]));
                         }
                     }
                 }
             }
         }
     }
-    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R, true});
+    reduce_group<2 * R>(acc, g, t.active, red, 0,
+                        ClaimFin{red, evals_out, nullptr, evals_out, {p.r[0], p.r[1], p.r[2]}, g.N, (uint32_t)R});
 }
 
 // ---------------------------------------------------------------- persistent phase tail
@@ -1610,6 +1648,14 @@ cudaError_t launch_eq(uint32_t* out, const EqArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+cudaError_t launch_scale_weights(uint64_t I, const uint32_t* mx_off, const uint4* w4, uint4* w4r, const uint32_t r[3],
+                                 int reps, cudaStream_t s) {
+    if (reps < 1 || reps > 3) return cudaErrorInvalidValue;
+    const uint4 rr = make_uint4(r[0], reps > 1 ? r[1] : 0u, reps > 2 ? r[2] : 0u, 0u);
+    k_scale_weights<<<grid_1d(I, 256), 256, 0, s>>>(I, mx_off, w4, w4r, rr);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* eqc, const uint4* mx_g,
                            const uint32_t* ax_off, const uint2* ax_g, uint4* a_out, uint4* w_out, uint32_t reps,
                            cudaStream_t s) {
@@ -1688,18 +1734,20 @@ uint32_t launch_stage_words(uint32_t* dst, const uint32_t* const* srcs, uint32_t
 
 cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* pairs,
                              const uint32_t* mx_off, const uint4* mx_g, const uint4* a4, const uint4* w4, const Geo& g,
-                             uint32_t block, uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
+                             uint32_t block, uint32_t ctas, RedScratch red, const uint32_t* claim,
+                             uint32_t* evals_out, cudaStream_t s) {
+    if (!claim) return cudaErrorInvalidValue;
     // the kernel's launch bound is 256 threads: wider tiles are narrowed to it
     Geo gb = g;
     if (block > 256) block = 256;
     while (gb.tpr > block && gb.tpr % 2 == 0) gb.tpr /= 2;
     if (gb.tpr > block) return cudaErrorInvalidValue;
     gb.rps = block / gb.tpr;
-    LaunchShape sh = row_shape(gb, npairs, block, ctas, 3 * reps);
+    LaunchShape sh = row_shape(gb, npairs, block, ctas, 2 * reps);
     const size_t ring = (size_t)kStages * kStageFields * sizeof(uint4) * block;
 #define GKR_HG0(RR)                                                                                                \
     k_hg_round0<RR><<<sh.grid, sh.block, hg0_smem<RR>(ring, sh.smem), s>>>(v, npairs, pairs, mx_off, mx_g, a4, w4, \
-                                                                          gb, red, evals_out)
+                                                                          gb, red, claim, evals_out)
     switch (reps) {
         case 1: GKR_HG0(1); break;
         case 2: GKR_HG0(2); break;
@@ -1711,13 +1759,13 @@ cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t npairs, const
 }
 
 cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* quads,
-                             const uint32_t* mx_off, const uint4* mx_g, const uint4* a4, const uint4* w4,
+                             const uint32_t* mx_off, const uint4* mx_g, const uint4* a4, const uint4* w4r,
                              const RoundPtrs& p, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
                              uint32_t* evals_out, cudaStream_t s) {
     if (quads && p.fdst[0]) return cudaErrorInvalidValue;  // stored folded copies need every pair
-    LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
+    LaunchShape sh = row_shape(g, npairs, block, ctas, 2 * reps);
 #define GKR_HG1(RR) \
-    k_hg_round1<RR><<<sh.grid, sh.block, sh.smem, s>>>(v, npairs, quads, mx_off, mx_g, a4, w4, p, g, red, evals_out)
+    k_hg_round1<RR><<<sh.grid, sh.block, sh.smem, s>>>(v, npairs, quads, mx_off, mx_g, a4, w4r, p, g, red, evals_out)
     switch (reps) {
         case 1: GKR_HG1(1); break;
         case 2: GKR_HG1(2); break;

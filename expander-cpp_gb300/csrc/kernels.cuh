@@ -136,22 +136,32 @@ cudaError_t launch_eq(uint32_t* out, const EqArgs& a, cudaStream_t s);
 // number of increments); *err receives the launch status.
 uint32_t launch_stage_words(uint32_t* dst, const uint32_t* const* srcs, uint32_t nsrc, uint64_t n, unsigned int* done,
                             cudaStream_t s, cudaError_t* err);
+// w4r[k].j = w4[k].j (1 - r_j) for the mul gates of even input rows, w4[k].j r_j for odd
+// rows (CSR-by-x offsets mx_off over I rows): the weights of launch_hg_round1.
+cudaError_t launch_scale_weights(uint64_t I, const uint32_t* mx_off, const uint4* w4, uint4* w4r, const uint32_t r[3],
+                                 int reps, cudaStream_t s);
 cudaError_t launch_weights(uint64_t I, uint64_t Gm, uint64_t O, const uint32_t* eqc, const uint4* mx_g,
                            const uint32_t* ax_off, const uint2* ax_g, uint4* a_out, uint4* w_out, uint32_t reps,
                            cudaStream_t s);
 // Phase-one hg (not stored) and the round-0 evaluations over `npairs` pairs of input rows:
 // pair i is (2q, 2q+1) with q = pairs[i], or q = i without a list (pairs = null).  Pairs
 // left out of the list must have no gate whose first input is in them (their hg is zero).
+// `claim` (R x N, device-readable, required) is the round's claim alpha v(rz1) + beta v(rz2)
+// per repetition and copy: the evaluations at 1 are the claim less those at 0.
 cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* pairs,
                              const uint32_t* mx_off, const uint4* mx_g, const uint4* a4, const uint4* w4, const Geo& g,
-                             uint32_t block, uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s);
+                             uint32_t block, uint32_t ctas, RedScratch red, const uint32_t* claim,
+                             uint32_t* evals_out, cudaStream_t s);
 // Phase-one round 1 rebuilding hg from the gate weights (no stored hg table): outputs
 // p.fdst[j] / p.hdst[j] (I/2 rows each; p.fdst[0] null: the folded copies are not stored),
 // challenges p.r[j]; npairs output pairs, pair i folding input rows 4q .. 4q+3 with
 // q = quads[i] (q = i without a list).  A list, which may leave out only groups of four rows
-// with no gate whose first input is in them, needs p.fdst[0] null.
+// with no gate whose first input is in them, needs p.fdst[0] null.  `evals_out` must hold
+// round 0's evaluations: the round's claim is round 0's polynomial at p.r[j], and the
+// evaluations at 1 are that claim less those at 0.  w4r: the gate weights scaled at p.r
+// (launch_scale_weights).
 cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* quads,
-                             const uint32_t* mx_off, const uint4* mx_g, const uint4* a4, const uint4* w4,
+                             const uint32_t* mx_off, const uint4* mx_g, const uint4* a4, const uint4* w4r,
                              const RoundPtrs& p, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
                              uint32_t* evals_out, cudaStream_t s);
 // Phase-one round 2 or 3 (k = round, a k_round with per-copy hg and fold) reading the

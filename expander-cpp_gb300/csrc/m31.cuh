@@ -64,4 +64,13 @@ GKR_HD uint32_t eval_at_two(uint32_t p0, uint32_t p1, uint32_t p2raw) {
     return sub(add(mul(p1, 6), mul(p0, 3)), mul(p2raw, 2));
 }
 
+// The degree-2 polynomial through (0, v0), (1, v1), (2, v2) evaluated at x: the claim the
+// next sumcheck round must meet (degree_2_eval, sumcheck_verifier_utils.hpp:10-18).  2^30 is
+// the inverse of 2 (2 * 2^30 = p + 1).
+GKR_HD uint32_t eval_degree2(uint32_t v0, uint32_t v1, uint32_t v2, uint32_t x) {
+    const uint32_t c2 = mul(1u << 30, add(sub(v2, add(v1, v1)), v0));
+    const uint32_t c1 = sub(sub(v1, v0), c2);
+    return add(v0, mul(add(mul(c2, x), c1), x));
+}
+
 }  // namespace m31

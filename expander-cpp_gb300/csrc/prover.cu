@@ -747,7 +747,7 @@ struct Workspace {
     uint32_t* sb[2] = {};
     uint32_t *eqc = nullptr, *eqrx = nullptr, *evals = nullptr, *vx = nullptr, *cv = nullptr;
     uint32_t* p2s = nullptr;  // 9R x N sums of phase-two rounds 0 and 1 (launch_p2_round01)
-    uint4 *a4 = nullptr, *w4 = nullptr;
+    uint4 *a4 = nullptr, *w4 = nullptr, *w4r = nullptr;
     unsigned long long* acc = nullptr;
     unsigned int* ticket = nullptr;
     unsigned int* flag = nullptr;
@@ -780,6 +780,7 @@ struct Workspace {
             eqrx = (uint32_t*)take(R * maxI * 4);
             a4 = (uint4*)take(maxI * 16);
             w4 = (uint4*)take(std::max<uint64_t>(C.max_mul, 1) * 16);
+            w4r = (uint4*)take(std::max<uint64_t>(C.max_mul, 1) * 16);
             p2s = (uint32_t*)take(27ull * N * 4);
         }
         eqc = (uint32_t*)take(R * maxO * 4);
@@ -813,6 +814,9 @@ struct Prover {
     Workspace ws;
     char* block = nullptr;
     std::vector<uint32_t*> vals;  // vals[l]: input of layer l; vals[L]: output of the last layer
+    // the layer's sum is alpha cv1 + beta cv2: the claimed values and zero for the output
+    // layer, then the previous layer's vx and vy (R x N each)
+    std::vector<uint32_t> cv1, cv2;
 
     Prover(gkrgpu_ctx& ctx, Lane& lane, const gkrgpu_circuit& circ, uint32_t n, int reps)
         : X(ctx), c(lane), C(circ), N(n), R(reps) {
@@ -900,7 +904,8 @@ struct Prover {
     // Round kernels publish their evaluations into the lane's mapped staging buffer.
     RedScratch red_mapped() const { return RedScratch{ws.acc, ws.ticket, c.done_d()}; }
     // The lane's mapped extra area: rows 0..1 of each repetition's last table (6N words), the
-    // claims (3N), vx (3N) and the input check flag.
+    // claimed values (3N), vx (3N), the input check flag, the tail kernels' error word and
+    // mailbox, and the claims of phase one's round 0 (3N).
     uint32_t* mapped(bool dev, uint64_t word) const {
         return reinterpret_cast<uint32_t*>(dev ? c.extra_d() : c.extra_h()) + word;
     }
@@ -911,6 +916,9 @@ struct Prover {
     // tail kernels: error word and challenge mailbox
     volatile uint32_t* err_h() const { return mapped(false, 12ull * N + 1); }
     volatile uint32_t* mbox_h() const { return mapped(false, 12ull * N + 64); }
+    // phase-one round 0's claims (R x N), after the mailbox
+    uint64_t claim_word() const { return align_up(12ull * N + 64 + kMboxWords, 64); }
+    uint64_t mapped_words() const { return claim_word() + 3ull * N; }
     bool tail_running = false;
     // Moves nsrc tables of n words into dst with k_stage_words (launch accounting as stage_words);
     // returns the number of completion increments when `done` is given.
@@ -932,7 +940,7 @@ struct Prover {
         block = static_cast<char*>(p);
         ws.plan(block, C, N, R, own_input, sumcheck);
         ck(cudaMemsetAsync(block + ws.zero_off, 0, ws.zero_bytes, c.stream), "cudaMemsetAsync");
-        c.ensure_mapped(9ull * N * 4, (12ull * N + 64 + kMboxWords) * 4);
+        c.ensure_mapped(9ull * N * 4, mapped_words() * 4);
         c.resync_done();
     }
 
@@ -1042,6 +1050,7 @@ struct Prover {
         uint32_t* v = vals[li];
         uint32_t* vxh = vx_h();
         std::vector<uint32_t> vy((size_t)R * N);
+        const uint64_t RN = (uint64_t)R * N;
 
         // phase one: eqc_j = alpha eq(rz1_j) + beta eq(rz2_j), gate weights, hg + round 0
         c.tag = ((uint32_t)li << 16) | (1u << 8);
@@ -1050,6 +1059,13 @@ struct Prover {
         c.launch(K_WEIGHTS, wb, [&] {
             return launch_weights(I, Ly.nmul, O, ws.eqc, Ly.mx_g, Ly.ax_off, Ly.ax_g, ws.a4, ws.w4, R, c.stream);
         });
+        // round 0's claims, alpha v(rz1) + beta v(rz2) per repetition and copy
+        // (sumcheck.hpp:129-132), while the eq table and the weights are computed
+        {
+            uint32_t* cl = mapped(false, claim_word());
+            for (uint64_t i = 0; i < RN; i++) cl[i] = m31::add(m31::mul(alpha, cv1[i]), m31::mul(beta, cv2[i]));
+            std::atomic_thread_fence(std::memory_order_seq_cst);
+        }
         // round 0 only reduces hg; round 1 rebuilds it (k_hg_round1), so no full-width hg
         // table is ever written
         // pairs of input rows without gates have hg = 0 and are skipped
@@ -1057,8 +1073,8 @@ struct Prover {
         const double hb = rb * (2.0 * np0 + Ly.nmul) + 32.0 * Ly.nmul + 44.0 * np0;
         c.launch(K_HG_ROUND0, hb, [&] {
             return launch_hg_round0(R, v, Ly.n_p1_pairs, Ly.p1_pairs, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4,
-                                    gk[K_HG_ROUND0], X.block, ck_ctas[K_HG_ROUND0], red_mapped(), c.evals_d(),
-                                    c.stream);
+                                    gk[K_HG_ROUND0], X.block, ck_ctas[K_HG_ROUND0], red_mapped(),
+                                    mapped(true, claim_word()), c.evals_d(), c.stream);
         });
         const uint32_t* vsrc[1] = {v};
         fetch(groups(K_HG_ROUND0), n == 1 ? vsrc : nullptr, true);
@@ -1104,8 +1120,11 @@ struct Prover {
                 const uint32_t* quads = refold1 ? Ly.p1_quads : nullptr;
                 const uint64_t nq = refold1 ? Ly.n_p1_quads : npairs;
                 const double vin = 4.0 * nq;
+                c.launch(K_WEIGHTS, 4.0 * (I + 1) + 32.0 * Ly.nmul, [&] {
+                    return launch_scale_weights(I, Ly.mx_off, ws.w4, ws.w4r, p.r, R, c.stream);
+                });
                 c.launch(K_HG_ROUND1, rb * (vin + Ly.nmul + f_out + (double)R * I / 2 - (double)R * Ly.h1_scalar_rows) + 32.0 * Ly.nmul + 20.0 * vin, [&] {
-                    return launch_hg_round1(R, v, nq, quads, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4, p, gk[K_HG_ROUND1],
+                    return launch_hg_round1(R, v, nq, quads, Ly.mx_off, Ly.mx_g, ws.a4, ws.w4r, p, gk[K_HG_ROUND1],
                                             X.block, ck_ctas[K_HG_ROUND1], red_mapped(), c.evals_d(), c.stream);
                 });
             } else if (k == 2 || k == 3) {
@@ -1264,6 +1283,9 @@ struct Prover {
             for (int j = 0; j < R; j++) cur_f[j] = p.fdst[j];
         }
         for (int j = 0; j < R; j++) t.append(vy.data() + (size_t)j * N, rowb);
+        // the next layer's sum is alpha vx + beta vy (gkr.hpp:113-119)
+        cv1.assign(vxh, vxh + RN);
+        cv2.swap(vy);
     }
 
     // Device front half of a proof: workspace, input upload and check, Circuit::evaluate of
@@ -1303,6 +1325,8 @@ struct Prover {
         c.sync();
         require_canonical();
         memcpy(claimed_v, cv_h(), R * rowb);
+        cv1.assign(claimed_v, claimed_v + (size_t)R * N);
+        cv2.assign((size_t)R * N, 0u);
 
         for (int li = (int)L - 1; li >= 0; li--) {
             sumcheck_layer(t, (size_t)li, rz1, rz2, alpha, beta, rx, ry);
