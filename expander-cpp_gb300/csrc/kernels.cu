@@ -452,6 +452,42 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(K) : "memory");
 }
 
+// ---------------------------------------------------------------- gathered gate terms
+// h_j += sum over mul gates k0 .. k1 - 1 of v[y_k] w_j[k] for the thread's four copies, each
+// product added unreduced below 2^32 (mac_lazy).  U gates per step: their gathers (a gate
+// index, then a row) are all in flight before the products (8 registers per extra gate).
+template <int R, int U>
+__device__ __forceinline__ void gate_terms(const uint32_t* __restrict__ v, const uint4* __restrict__ mx_g,
+                                           const uint4* __restrict__ w4, uint32_t k0, uint32_t k1, uint32_t N,
+                                           uint32_t lane0, uint32_t (&h)[R][4]) {
+    uint32_t k = k0;
+    for (; U > 1 && k + U <= k1; k += U) {
+        uint32_t y[U];
+        uint4 w[U], vy[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) y[u] = __ldg(&mx_g[k + u].x);
+#pragma unroll
+        for (int u = 0; u < U; u++) w[u] = __ldg(w4 + k + u);
+#pragma unroll
+        for (int u = 0; u < U; u++) vy[u] = ld4(v, y[u], N, lane0);
+#pragma unroll
+        for (int u = 0; u < U; u++)
+#pragma unroll
+            for (int j = 0; j < R; j++)
+#pragma unroll
+                for (int l = 0; l < 4; l++) h[j][l] = m31::mac_lazy(h[j][l], comp(vy[u], l), comp(w[u], j));
+    }
+    for (; k < k1; k++) {
+        const uint32_t y = __ldg(&mx_g[k].x);
+        const uint4 w = __ldg(w4 + k);
+        const uint4 vy = ld4(v, y, N, lane0);
+#pragma unroll
+        for (int j = 0; j < R; j++)
+#pragma unroll
+            for (int l = 0; l < 4; l++) h[j][l] = m31::mac_lazy(h[j][l], comp(vy, l), comp(w, j));
+    }
+}
+
 // ---------------------------------------------------------------- phase one: hg build + round 0
 // For each pair (x0, x1) = (2i, 2i+1): hg_j[x] = a_j[x] + sum over mul gates (x, y, k) of
 // v[y] * w_j[k], then the round-0 sums of v(x) hg_j(x).  hg is not stored: round 1
@@ -467,9 +503,10 @@ __device__ __forceinline__ void cp_async_wait() {
 constexpr int kStages = 3;
 constexpr int kStageFields = 5;  // v(2i), v(2i+1), a(2i), a(2i+1), (off(2i), off(2i+1), off(2i+2))
 constexpr int kMaxStagedSmem = kStages * kStageFields * 16 * 256;
+constexpr int kHg0Gates = 2, kHg1Gates = 2;  // gathers in flight per thread (gate_terms)
 
 template <int R>
-__global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict__ v, uint64_t npairs,
+__global__ void __launch_bounds__(256, 2) k_hg_round0(const uint32_t* __restrict__ v, uint64_t npairs,
                                                       const uint32_t* __restrict__ pairs,
                                                       const uint32_t* __restrict__ mx_off,
                                                       const uint4* __restrict__ mx_g, const uint4* __restrict__ a4,
@@ -486,15 +523,7 @@ __global__ void __launch_bounds__(256, 3) k_hg_round0(const uint32_t* __restrict
     // adds the mul-gate terms of input row x (gates k0 .. k1) to h, canonical before and after
     auto gates = [&](uint32_t k0, uint32_t k1, uint32_t (&h)[R][4]) {
         if (k0 == k1) return;
-        for (uint32_t k = k0; k < k1; k++) {
-            const uint32_t y = __ldg(&mx_g[k].x);
-            const uint4 w = __ldg(w4 + k);
-            const uint4 vy = ld4(v, y, g.N, t.lane0);
-#pragma unroll
-            for (int j = 0; j < R; j++)
-#pragma unroll
-                for (int l = 0; l < 4; l++) h[j][l] = m31::mac_lazy(h[j][l], comp(vy, l), comp(w, j));
-        }
+        gate_terms<R, kHg0Gates>(v, mx_g, w4, k0, k1, g.N, t.lane0, h);
 #pragma unroll
         for (int j = 0; j < R; j++)
 #pragma unroll
@@ -632,15 +661,7 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
                     for (int l = 0; l < 4; l++) h[j][l] = hs;
                 }
                 if (off[2 * s] != off[2 * s + 2]) {
-                    for (uint32_t k = off[2 * s]; k < off[2 * s + 2]; k++) {
-                        const uint32_t y = __ldg(&mx_g[k].x);
-                        const uint4 w = __ldg(w4r + k);
-                        const uint4 vy = ld4(v, y, g.N, t.lane0);
-#pragma unroll
-                        for (int j = 0; j < R; j++)
-#pragma unroll
-                            for (int l = 0; l < 4; l++) h[j][l] = m31::mac_lazy(h[j][l], comp(vy, l), comp(w, j));
-                    }
+                    gate_terms<R, kHg1Gates>(v, mx_g, w4r, off[2 * s], off[2 * s + 2], g.N, t.lane0, h);
 #pragma unroll
                     for (int j = 0; j < R; j++)
 #pragma unroll
