@@ -371,6 +371,11 @@ struct RoundFin {
             out[(size_t)(3 * j) * N + lane] = p0;
             out[(size_t)(3 * j + 1) * N + lane] = p1;
             out[(size_t)(3 * j + 2) * N + lane] = p2;
+            if (red.evals_dev) {
+                red.evals_dev[(size_t)(3 * j) * N + lane] = p0;
+                red.evals_dev[(size_t)(3 * j + 1) * N + lane] = p1;
+                red.evals_dev[(size_t)(3 * j + 2) * N + lane] = p2;
+            }
         }
     }
 };
@@ -378,32 +383,44 @@ struct RoundFin {
 // Round evaluations from two sums per repetition, p0 and p2raw: p1 is the round's claim less
 // p0 (an honest prover's round polynomial meets p0 + p1 = claim, the verifier's check in
 // sumcheck.hpp:152, so p1 is the same field element as its direct sum).  The claim is
-// `claim` (R x N, written by the host before the launch), or with `prev` the previous
-// round's polynomial at its challenge r_j, eval_degree2 of its three evaluations: `prev` is
-// the buffer this finisher overwrites, each lane read before it is written.
+// `claim` (R x N, written by the host before the launch), or without it the previous
+// round's polynomial at its challenge r_j, eval_degree2 of the three evaluations in
+// red.evals_dev, which this finisher then overwrites (each lane read before it is written).
+// With vx (phase two) the sums are multiplied by v(rx) first; the claim is of the multiplied
+// polynomial.
 struct ClaimFin {
     RedScratch red;
     uint32_t* out;            // R x 3 x N
     const uint32_t* claim;    // R x N, or null
-    const uint32_t* prev;     // R x 3 x N, or null
     uint32_t r[3];
     uint32_t N, reps;
+    const uint32_t* vx = nullptr;  // R x N, or null
     __device__ void operator()(uint32_t lane) const {
+        uint32_t* dev = red.evals_dev;
         for (uint32_t j = 0; j < reps; j++) {
             uint32_t cl;
-            if (prev) {
-                const uint32_t rj = j == 0 ? r[0] : (j == 1 ? r[1] : r[2]);
-                cl = m31::eval_degree2(__ldcv(prev + (size_t)(3 * j) * N + lane),
-                                       __ldcv(prev + (size_t)(3 * j + 1) * N + lane),
-                                       __ldcv(prev + (size_t)(3 * j + 2) * N + lane), rj);
-            } else {
+            if (claim) {
                 cl = __ldcv(claim + (size_t)j * N + lane);
+            } else {
+                const uint32_t rj = j == 0 ? r[0] : (j == 1 ? r[1] : r[2]);
+                cl = m31::eval_degree2(dev[(size_t)(3 * j) * N + lane], dev[(size_t)(3 * j + 1) * N + lane],
+                                       dev[(size_t)(3 * j + 2) * N + lane], rj);
             }
-            const uint32_t p0 = take(red, 2 * j, N, lane), p2raw = take(red, 2 * j + 1, N, lane);
-            const uint32_t p1 = sub(cl, p0);
+            uint32_t p0 = take(red, 2 * j, N, lane), p2raw = take(red, 2 * j + 1, N, lane);
+            if (vx) {
+                const uint32_t x = vx[(size_t)j * N + lane];
+                p0 = mul(p0, x);
+                p2raw = mul(p2raw, x);
+            }
+            const uint32_t p1 = sub(cl, p0), p2 = m31::eval_at_two(p0, p1, p2raw);
             out[(size_t)(3 * j) * N + lane] = p0;
             out[(size_t)(3 * j + 1) * N + lane] = p1;
-            out[(size_t)(3 * j + 2) * N + lane] = m31::eval_at_two(p0, p1, p2raw);
+            out[(size_t)(3 * j + 2) * N + lane] = p2;
+            if (dev) {
+                dev[(size_t)(3 * j) * N + lane] = p0;
+                dev[(size_t)(3 * j + 1) * N + lane] = p1;
+                dev[(size_t)(3 * j + 2) * N + lane] = p2;
+            }
         }
     }
 };
@@ -426,6 +443,17 @@ __device__ __forceinline__ void accum_pair(uint32_t (&acc)[3][4], const uint32_t
         acc[0][l] = m31::mac_lazy(acc[0][l], f0[l], h0[l]);
         acc[1][l] = m31::mac_lazy(acc[1][l], f1[l], h1[l]);
         acc[2][l] = m31::mac_lazy(acc[2][l], add(f0[l], f1[l]), add(h0[l], h1[l]));
+    }
+}
+
+// p0 += f0 h0 and p2raw += (f0 + f1)(h0 + h1) for four copies (mac_lazy): the two sums of a
+// round whose p1 comes from its claim (ClaimFin).
+__device__ __forceinline__ void accum_pair2(uint32_t (&acc)[2][4], const uint32_t (&f0)[4], const uint32_t (&f1)[4],
+                                            const uint32_t (&h0)[4], const uint32_t (&h1)[4]) {
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+        acc[0][l] = m31::mac_lazy(acc[0][l], f0[l], h0[l]);
+        acc[1][l] = m31::mac_lazy(acc[1][l], add(f0[l], f1[l]), add(h0[l], h1[l]));
     }
 }
 
@@ -605,7 +633,7 @@ __global__ void __launch_bounds__(256, 2) k_hg_round0(const uint32_t* __restrict
     __syncthreads();  // the ring is reused as the reduction's scratch (sums below 2^32 are
                       // added as they are: the finisher reduces the 64-bit totals)
     reduce_group<2 * R>(acc, g, t.active, red, 0,
-                        ClaimFin{red, evals_out, claim, nullptr, {0u, 0u, 0u}, g.N, (uint32_t)R});
+                        ClaimFin{red, evals_out, claim, {0u, 0u, 0u}, g.N, (uint32_t)R});
 }
 
 // ---------------------------------------------------------------- phase one, round 1
@@ -692,7 +720,7 @@ __global__ void __launch_bounds__(256) k_hg_round1(const uint32_t* __restrict__ 
         }
     }
     reduce_group<2 * R>(acc, g, t.active, red, 0,
-                        ClaimFin{red, evals_out, nullptr, evals_out, {p.r[0], p.r[1], p.r[2]}, g.N, (uint32_t)R});
+                        ClaimFin{red, evals_out, nullptr, {p.r[0], p.r[1], p.r[2]}, g.N, (uint32_t)R});
 }
 
 // ---------------------------------------------------------------- persistent phase tail
@@ -897,7 +925,7 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, con
     uint32_t* __restrict__ fd = j == 0 ? p.fdst[0] : (j == 1 ? p.fdst[1] : p.fdst[2]);
     uint32_t* __restrict__ hd = j == 0 ? p.hdst[0] : (j == 1 ? p.hdst[1] : p.hdst[2]);
     const uint32_t r = j == 0 ? p.r[0] : (j == 1 ? p.r[1] : p.r[2]);
-    uint32_t acc[3][4] = {};
+    uint32_t acc[2][4] = {};  // p0, p2raw
     if (t.active) {
         uint64_t i = (uint64_t)cx * g.rps + t.rs;
         const uint64_t step = (uint64_t)nx * g.rps;
@@ -916,7 +944,7 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, con
                 }
                 st4(fd, 2 * ii, g.N, t.lane0, mk4(f0));
                 st4(fd, 2 * ii + 1, g.N, t.lane0, mk4(f1));
-                accum_pair(acc, f0, f1, h0, h1);
+                accum_pair2(acc, f0, f1, h0, h1);
             };
             for (; i + step < npairs; i += 2 * step) {
                 uint4 a[4], b[4];
@@ -1003,10 +1031,12 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrs p, uint64_t npairs, con
                     for (int l = 0; l < 4; l++) { h0[l] = s.x; h1[l] = s.y; }
                 }
             }
-            accum_pair(acc, f0, f1, h0, h1);
+            accum_pair2(acc, f0, f1, h0, h1);
         }
     }
-    reduce_group<3>(acc, g, t.active, red, 3 * j, RoundFin{red, evals_out, LANE_HG ? nullptr : vx, g.N, reps});
+    reduce_group<2>(acc, g, t.active, red, 2 * j,
+                    ClaimFin{red, evals_out, nullptr, {p.r[0], p.r[1], p.r[2]}, g.N, reps,
+                             LANE_HG ? nullptr : vx});
 }
 
 // Phase-one round 2 after a round 1 that stored no folded copies of the layer input, with
@@ -1023,9 +1053,9 @@ __global__ void __launch_bounds__(256) k_p1_round2(RoundPtrs p, uint64_t npairs,
                                                    uint32_t* evals_out) {
     const TileIdx t = tile_idx(g);
     const uint32_t* __restrict__ v = p.fsrc[0];
-    uint32_t acc[3 * R][4];
+    uint32_t acc[2 * R][4];  // 2j: p0, 2j + 1: p2raw
 #pragma unroll
-    for (int c = 0; c < 3 * R; c++)
+    for (int c = 0; c < 2 * R; c++)
 #pragma unroll
         for (int l = 0; l < 4; l++) acc[c][l] = 0u;
     if (t.active) {
@@ -1068,20 +1098,20 @@ __global__ void __launch_bounds__(256) k_p1_round2(RoundPtrs p, uint64_t npairs,
 #pragma unroll
                     for (int l = 0; l < 4; l++) {
                         if (s == 0) {
-                            acc[3 * j][l] = m31::mac_lazy(acc[3 * j][l], f[l], h[l]);
+                            acc[2 * j][l] = m31::mac_lazy(acc[2 * j][l], f[l], h[l]);
                             fe[j][l] = f[l];
                             he[j][l] = h[l];
                         } else {
-                            acc[3 * j + 1][l] = m31::mac_lazy(acc[3 * j + 1][l], f[l], h[l]);
-                            acc[3 * j + 2][l] =
-                                m31::mac_lazy(acc[3 * j + 2][l], add(fe[j][l], f[l]), add(he[j][l], h[l]));
+                            acc[2 * j + 1][l] =
+                                m31::mac_lazy(acc[2 * j + 1][l], add(fe[j][l], f[l]), add(he[j][l], h[l]));
                         }
                     }
                 }
             }
         }
     }
-    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, nullptr, g.N, (uint32_t)R});
+    reduce_group<2 * R>(acc, g, t.active, red, 0,
+                        ClaimFin{red, evals_out, nullptr, {p.r[0], p.r[1], p.r[2]}, g.N, (uint32_t)R});
 }
 
 // Shared-source rounds (phase-1 round 1, phase-2 rounds 0 and 1) with every repetition in
@@ -1092,7 +1122,7 @@ __global__ void __launch_bounds__(256) k_round_shared(RoundPtrs p, uint64_t npai
                                                       Geo g, RedScratch red, uint32_t* evals_out) {
     const TileIdx t = tile_idx(g);
     const uint32_t* __restrict__ fs = p.fsrc[0];
-    uint32_t acc[3 * R][4] = {};
+    uint32_t acc[2 * R][4] = {};  // 2j: p0, 2j + 1: p2raw
     if (t.active) {
         for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
             uint4 a[4];
@@ -1145,14 +1175,15 @@ __global__ void __launch_bounds__(256) k_round_shared(RoundPtrs p, uint64_t npai
                 }
 #pragma unroll
                 for (int l = 0; l < 4; l++) {
-                    acc[3 * j][l] = add(acc[3 * j][l], mul(f0[l], h0[l]));
-                    acc[3 * j + 1][l] = add(acc[3 * j + 1][l], mul(f1[l], h1[l]));
-                    acc[3 * j + 2][l] = add(acc[3 * j + 2][l], mul(add(f0[l], f1[l]), add(h0[l], h1[l])));
+                    acc[2 * j][l] = add(acc[2 * j][l], mul(f0[l], h0[l]));
+                    acc[2 * j + 1][l] = add(acc[2 * j + 1][l], mul(add(f0[l], f1[l]), add(h0[l], h1[l])));
                 }
             }
         }
     }
-    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, LANE_HG ? nullptr : vx, g.N, (uint32_t)R});
+    reduce_group<2 * R>(acc, g, t.active, red, 0,
+                        ClaimFin{red, evals_out, nullptr, {p.r[0], p.r[1], p.r[2]}, g.N, (uint32_t)R,
+                                 LANE_HG ? nullptr : vx});
 }
 
 // Phase-two round 2 from the layer input: round 1 stored only its folded scalar tables, not
@@ -1166,9 +1197,9 @@ __global__ void __launch_bounds__(256) k_p2_round2(RoundPtrs p, uint64_t npairs,
                                                    Geo g, RedScratch red, uint32_t* evals_out) {
     const TileIdx t = tile_idx(g);
     const uint32_t* __restrict__ fs = p.fsrc[0];
-    uint32_t acc[3 * R][4];
+    uint32_t acc[2 * R][4];  // 2j: p0, 2j + 1: p2raw
 #pragma unroll
-    for (int c = 0; c < 3 * R; c++)
+    for (int c = 0; c < 2 * R; c++)
 #pragma unroll
         for (int l = 0; l < 4; l++) acc[c][l] = 0u;
     if (t.active) {
@@ -1198,18 +1229,18 @@ __global__ void __launch_bounds__(256) k_p2_round2(RoundPtrs p, uint64_t npairs,
                 const uint32_t hs = add(s0, s1);
 #pragma unroll
                 for (int l = 0; l < 4; l++) {
-                    acc[3 * j][l] = m31::mac_lazy(acc[3 * j][l], f0[l], h0[l]);
-                    acc[3 * j + 1][l] = m31::mac_lazy(acc[3 * j + 1][l], f1[l], h1[l]);
-                    acc[3 * j + 2][l] = m31::mac_lazy(acc[3 * j + 2][l], add(f0[l], f1[l]), hs);
+                    acc[2 * j][l] = m31::mac_lazy(acc[2 * j][l], f0[l], h0[l]);
+                    acc[2 * j + 1][l] = m31::mac_lazy(acc[2 * j + 1][l], add(f0[l], f1[l]), hs);
                 }
             }
         }
     }
 #pragma unroll
-    for (int c = 0; c < 3 * R; c++)
+    for (int c = 0; c < 2 * R; c++)
 #pragma unroll
         for (int l = 0; l < 4; l++) acc[c][l] = m31::from_u32(acc[c][l]);
-    reduce_group<3 * R>(acc, g, t.active, red, 0, RoundFin{red, evals_out, vx, g.N, (uint32_t)R});
+    reduce_group<2 * R>(acc, g, t.active, red, 0,
+                        ClaimFin{red, evals_out, nullptr, {p.r[0], p.r[1], p.r[2]}, g.N, (uint32_t)R, vx});
 }
 
 // x == x mod p for any 64-bit x: x = hi 2^32 + lo and 2^32 == 2 (mod 2^31 - 1), so the result
@@ -1484,7 +1515,7 @@ struct P1Fold {
 
 __global__ void __launch_bounds__(256) k_p2_round1_fin(const uint32_t* __restrict__ sums, const uint32_t* __restrict__ vx,
                                                        P1Fold f, uint64_t ngroups, uint32_t N, uint32_t reps,
-                                                       uint32_t* evals_out, unsigned int* done) {
+                                                       uint32_t* evals_out, uint32_t* evals_dev, unsigned int* done) {
     const uint32_t tid = threadIdx.x, B = blockDim.x;
     if (blockIdx.x == 0) {
         for (uint32_t j = 0; j < reps; j++) {
@@ -1502,9 +1533,15 @@ __global__ void __launch_bounds__(256) k_p2_round1_fin(const uint32_t* __restric
                 const uint32_t p1 = add(add(mul(c0, m[3]), mul(c1, m[5])), mul(c2, m[4]));
                 const uint32_t p2raw = add(add(mul(c0, m[6]), mul(c1, m[8])), mul(c2, m[7]));
                 const uint32_t x = __ldg(vx + (size_t)j * N + lane);
-                evals_out[(size_t)(3 * j) * N + lane] = mul(p0, x);
-                evals_out[(size_t)(3 * j + 1) * N + lane] = mul(p1, x);
-                evals_out[(size_t)(3 * j + 2) * N + lane] = mul(m31::eval_at_two(p0, p1, p2raw), x);
+                const uint32_t e0 = mul(p0, x), e1 = mul(p1, x), e2 = mul(m31::eval_at_two(p0, p1, p2raw), x);
+                evals_out[(size_t)(3 * j) * N + lane] = e0;
+                evals_out[(size_t)(3 * j + 1) * N + lane] = e1;
+                evals_out[(size_t)(3 * j + 2) * N + lane] = e2;
+                if (evals_dev) {
+                    evals_dev[(size_t)(3 * j) * N + lane] = e0;
+                    evals_dev[(size_t)(3 * j + 1) * N + lane] = e1;
+                    evals_dev[(size_t)(3 * j + 2) * N + lane] = e2;
+                }
             }
         }
         if (done) {
@@ -1611,7 +1648,7 @@ uint32_t grid_1d(uint64_t n, uint32_t block) {
 
 // Row tile with repetition-split CTAs: gridDim.x = reps x row chunks.
 LaunchShape rep_shape(const Geo& g, uint64_t rows, uint32_t block, uint32_t ctas_cap, uint32_t reps) {
-    LaunchShape s = row_shape(g, rows, block, ctas_cap / reps, 3);
+    LaunchShape s = row_shape(g, rows, block, ctas_cap / reps, 2);
     s.grid.x *= reps;
     return s;
 }
@@ -1784,6 +1821,7 @@ cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const
                              const RoundPtrs& p, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
                              uint32_t* evals_out, cudaStream_t s) {
     if (quads && p.fdst[0]) return cudaErrorInvalidValue;  // stored folded copies need every pair
+    if (!red.evals_dev) return cudaErrorInvalidValue;       // the claim is round 0's polynomial
     LaunchShape sh = row_shape(g, npairs, block, ctas, 2 * reps);
 #define GKR_HG1(RR) \
     k_hg_round1<RR><<<sh.grid, sh.block, sh.smem, s>>>(v, npairs, quads, mx_off, mx_g, a4, w4r, p, g, red, evals_out)
@@ -1835,9 +1873,10 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, co
         }
         return cudaGetLastError();
     }
+    if (!red.evals_dev) return cudaErrorInvalidValue;  // fold rounds take their claim from it
     if (shared_src) {
         // one read of the shared layer input for all repetitions
-        LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
+        LaunchShape sh = row_shape(g, npairs, block, ctas, 2 * reps);
 #define GKR_SHARED(RR, LH, FO) k_round_shared<RR, LH, FO><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out)
 #define GKR_SHARED_R(RR)                                  \
     if (lane_hg) GKR_SHARED(RR, true, true);              \
@@ -1866,7 +1905,8 @@ cudaError_t launch_round(int reps, bool shared_src, bool lane_hg, bool fold_, co
 
 cudaError_t launch_round_hr(int round, int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
                             uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
-    if (reps < 1 || reps > 3 || !p.hoff || !p.ha || (round != 2 && round != 3)) return cudaErrorInvalidValue;
+    if (reps < 1 || reps > 3 || !p.hoff || !p.ha || (round != 2 && round != 3) || !red.evals_dev)
+        return cudaErrorInvalidValue;
     LaunchShape sh = rep_shape(g, npairs, block, ctas, reps);
     if (round == 2)
         k_round<false, true, true, 1><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, nullptr, g, reps, red, evals_out);
@@ -1877,8 +1917,8 @@ cudaError_t launch_round_hr(int round, int reps, const RoundPtrs& p, uint64_t np
 
 cudaError_t launch_p1_round2(int reps, const RoundPtrs& p, uint64_t npairs, const Geo& g, uint32_t block,
                              uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
-    if (!p.hoff || !p.ha) return cudaErrorInvalidValue;
-    LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
+    if (!p.hoff || !p.ha || !red.evals_dev) return cudaErrorInvalidValue;
+    LaunchShape sh = row_shape(g, npairs, block, ctas, 2 * reps);
     switch (reps) {
         case 1: k_p1_round2<1><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, g, red, evals_out); break;
         case 2: k_p1_round2<2><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, g, red, evals_out); break;
@@ -1890,7 +1930,8 @@ cudaError_t launch_p1_round2(int reps, const RoundPtrs& p, uint64_t npairs, cons
 
 cudaError_t launch_p2_round2(int reps, const RoundPtrs& p, uint64_t npairs, const uint32_t* vx, const Geo& g,
                              uint32_t block, uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
-    LaunchShape sh = row_shape(g, npairs, block, ctas, 3 * reps);
+    if (!red.evals_dev) return cudaErrorInvalidValue;
+    LaunchShape sh = row_shape(g, npairs, block, ctas, 2 * reps);
     switch (reps) {
         case 1: k_p2_round2<1><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out); break;
         case 2: k_p2_round2<2><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out); break;
@@ -1944,7 +1985,7 @@ cudaError_t launch_p2_round01(int reps, const uint32_t* v, const uint32_t* const
 
 cudaError_t launch_p2_round1_fin(int reps, const uint32_t* sums, const uint32_t* vx, const uint32_t* const* s,
                                  uint32_t* const* sd, const uint32_t* r, uint64_t ngroups, uint32_t N,
-                                 uint32_t* evals_out, unsigned int* done, cudaStream_t st) {
+                                 uint32_t* evals_out, uint32_t* evals_dev, unsigned int* done, cudaStream_t st) {
     if (reps < 1 || reps > 3) return cudaErrorInvalidValue;
     P1Fold f;
     for (int j = 0; j < 3; j++) {
@@ -1953,7 +1994,8 @@ cudaError_t launch_p2_round1_fin(int reps, const uint32_t* sums, const uint32_t*
         f.r[j] = j < reps ? r[j] : 0u;
     }
     const uint32_t fold_blocks = grid_1d((uint64_t)reps * ngroups, 256);
-    k_p2_round1_fin<<<1 + fold_blocks, 256, 0, st>>>(sums, vx, f, ngroups, N, (uint32_t)reps, evals_out, done);
+    k_p2_round1_fin<<<1 + fold_blocks, 256, 0, st>>>(sums, vx, f, ngroups, N, (uint32_t)reps, evals_out, evals_dev,
+                                                      done);
     return cudaGetLastError();
 }
 

@@ -23,6 +23,9 @@ struct RedScratch {
     // Optional completion counter in host-mapped memory: each lane group's finishing CTA
     // increments it (system scope) after its results are visible to the host.
     unsigned int* done = nullptr;
+    // Optional device copy of the published round evaluations (R x 3 x N): the round kernels
+    // that take p1 from their claim read the previous round's evaluations here.
+    uint32_t* evals_dev = nullptr;
 };
 
 struct EqArgs {
@@ -156,14 +159,19 @@ cudaError_t launch_hg_round0(int reps, const uint32_t* v, uint64_t npairs, const
 // p.fdst[j] / p.hdst[j] (I/2 rows each; p.fdst[0] null: the folded copies are not stored),
 // challenges p.r[j]; npairs output pairs, pair i folding input rows 4q .. 4q+3 with
 // q = quads[i] (q = i without a list).  A list, which may leave out only groups of four rows
-// with no gate whose first input is in them, needs p.fdst[0] null.  `evals_out` must hold
-// round 0's evaluations: the round's claim is round 0's polynomial at p.r[j], and the
-// evaluations at 1 are that claim less those at 0.  w4r: the gate weights scaled at p.r
+// with no gate whose first input is in them, needs p.fdst[0] null.  red.evals_dev (required)
+// must hold round 0's evaluations: the round's claim is round 0's polynomial at p.r[j], and
+// the evaluations at 1 are that claim less those at 0.  w4r: the gate weights scaled at p.r
 // (launch_scale_weights).
 cudaError_t launch_hg_round1(int reps, const uint32_t* v, uint64_t npairs, const uint32_t* quads,
                              const uint32_t* mx_off, const uint4* mx_g, const uint4* a4, const uint4* w4r,
                              const RoundPtrs& p, const Geo& g, uint32_t block, uint32_t ctas, RedScratch red,
                              uint32_t* evals_out, cudaStream_t s);
+// The fold rounds below (launch_round_hr, launch_p1_round2, launch_p2_round2 and
+// launch_round with fold) sum p0 and p2raw only: red.evals_dev (required) must hold the
+// previous round's evaluations in the same phase, whose polynomial at p.r[j] is the round's
+// claim, and the evaluations at 1 are that claim less those at 0.  Every round kernel writes
+// its evaluations to red.evals_dev as well as to evals_out when red.evals_dev is given.
 // Phase-one round 2 or 3 (k = round, a k_round with per-copy hg and fold) reading the
 // previous round's stored hg rows and recomputing the copy-independent ones (p.hoff, p.ha,
 // p.hr); round 2 in turn does not store its copy-independent output rows.
@@ -195,11 +203,11 @@ cudaError_t launch_p2_round01(int reps, const uint32_t* v, const uint32_t* const
                               RedScratch red, uint32_t* evals_out, uint32_t* sums_out, cudaStream_t st);
 uint32_t p2_round01_groups(uint32_t N);
 // Phase-two round 1 from those sums at the round-0 challenges r[j]: evaluations to evals_out
-// (one completion count on done), and the scalar tables s[j] folded into sd[j] (2 ngroups
-// entries each) for round 2.
+// and evals_dev (when given; one completion count on done), and the scalar tables s[j]
+// folded into sd[j] (2 ngroups entries each) for round 2.
 cudaError_t launch_p2_round1_fin(int reps, const uint32_t* sums, const uint32_t* vx, const uint32_t* const* s,
                                  uint32_t* const* sd, const uint32_t* r, uint64_t ngroups, uint32_t N,
-                                 uint32_t* evals_out, unsigned int* done, cudaStream_t st);
+                                 uint32_t* evals_out, uint32_t* evals_dev, unsigned int* done, cudaStream_t st);
 // launch_s_build plus the pair sums t_j(i) = (s_j(4i) + s_j(4i+2), s_j(4i+1) + s_j(4i+3),
 // s_j(4i) + s_j(4i+1), s_j(4i+2) + s_j(4i+3)) into t_out (4 I/4 entries, stride s_stride);
 // I and s_stride multiples of 4.

@@ -901,8 +901,9 @@ struct Prover {
     }
 
     RedScratch red() const { return RedScratch{ws.acc, ws.ticket}; }
-    // Round kernels publish their evaluations into the lane's mapped staging buffer.
-    RedScratch red_mapped() const { return RedScratch{ws.acc, ws.ticket, c.done_d()}; }
+    // Round kernels publish their evaluations into the lane's mapped staging buffer and keep a
+    // device copy (ws.evals), from which the next round takes its claim.
+    RedScratch red_mapped() const { return RedScratch{ws.acc, ws.ticket, c.done_d(), ws.evals}; }
     // The lane's mapped extra area: rows 0..1 of each repetition's last table (6N words), the
     // claimed values (3N), vx (3N), the input check flag, the tail kernels' error word and
     // mailbox, and the claims of phase one's round 0 (3N).
@@ -1205,8 +1206,8 @@ struct Prover {
             uint32_t* sd[3] = {ws.sb[1], ws.sb[1] + sstride, ws.sb[1] + 2 * sstride};
             uint32_t r0[3] = {ry[0][0], R > 1 ? ry[1][0] : 0u, R > 2 ? ry[2][0] : 0u};
             c.launch(K_ROUND_SCALAR, 4.0 * 9 * R * N + 4.0 * R * N + 6.0 * R * I, [&] {
-                return launch_p2_round1_fin(R, ws.p2s, ws.vx, sj, sd, r0, ngroups, N, c.evals_d(), c.done_d(),
-                                            c.stream);
+                return launch_p2_round1_fin(R, ws.p2s, ws.vx, sj, sd, r0, ngroups, N, c.evals_d(), ws.evals,
+                                            c.done_d(), c.stream);
             });
             fetch(1, nullptr, false);
             transcript_round(t, ry, 1, false, false, vy.data());
