@@ -16,6 +16,8 @@ __constant__ uint32_t kOne[8] = {0x4ffffffbu, 0xac96341cu, 0x9f60cd29u, 0x36fc76
                                  0x7879462eu, 0x666ea36fu, 0x9a07df2fu, 0x0e0a77c1u};  // 2^256 mod r
 __constant__ uint32_t kR2[8] = {0xae216da7u, 0x1bb8e645u, 0xe35c59e3u, 0x53fe3ab1u,
                                 0x53bb8085u, 0x8c49833du, 0x7f4e44a5u, 0x0216d0b1u};  // 2^512 mod r
+__constant__ uint32_t kInv2M[8] = {0x1ffffffeu, 0x783c14d8u, 0x0c8d1eddu, 0xaf982f6fu,
+                                   0xfcfd4f45u, 0x8f5f7492u, 0x3d9cbfacu, 0x1f37631au};  // (r + 1) / 2 * 2^256 mod r
 
 __device__ __forceinline__ Fr zero() {
     Fr z;
@@ -377,6 +379,7 @@ struct RoundFinBn {
     uint32_t* out;  // 3 x N x 8 limbs, canonical
     const uint32_t* vx;
     uint32_t N;
+    uint32_t* dev = nullptr;  // device copy of out, or null
     __device__ __noinline__ void operator()(uint32_t c, uint32_t lane, const Fr* t, uint32_t tpr) const {
         Fr v;
         if (c < 2) {
@@ -390,6 +393,68 @@ struct RoundFinBn {
         }
         if (vx) v = mul(v, ldf(vx, 0, N, lane));
         stf(out, c, N, lane, v);
+        if (dev) stf(dev, c, N, lane, v);
+    }
+};
+
+// Element of a host-written table read past the caches (each limb fetched again).
+__device__ __forceinline__ Fr ldf_cv(const uint32_t* base, uint32_t N, uint32_t lane) {
+    Fr f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) f.l[k] = __ldcv(base + (size_t)lane * 8 + k);
+    return f;
+}
+
+// The round's evaluations from two components per lane, p0 (t[0]) and p2raw (t[tpr]): p1 is
+// the round's claim less p0 (an honest prover's round polynomial meets p0 + p1 = claim, the
+// verifier's check in sumcheck.hpp:152).  The claim is `claim` (N x 8 words, host-written),
+// or the previous round's polynomial at its challenge r (Montgomery form), degree_2_eval
+// (sumcheck_verifier_utils.hpp:10-18) of its evaluations in `prev`.  Component 0 writes the
+// evaluations at 0 and 1, component 1 the one at 2; with vx (phase two) the sums are
+// multiplied by v(rx) first.  Canonical values times Montgomery forms give canonical values.
+struct ClaimFinBn {
+    uint32_t* out;          // 3 x N x 8 limbs, canonical
+    uint32_t* dev;          // device copy of out, or null
+    const uint32_t* claim;  // N x 8, or null
+    const uint32_t* prev;   // 3 x N x 8, or null
+    const uint32_t* vx;
+    Fr r;
+    uint32_t N;
+    __device__ __noinline__ void operator()(uint32_t c, uint32_t lane, const Fr* t, uint32_t tpr) const {
+        Fr cl;
+        if (claim) {
+            cl = ldf_cv(claim, N, lane);
+        } else {
+            const Fr v0 = ldf(prev, 0, N, lane), v1 = ldf(prev, 1, N, lane), v2 = ldf(prev, 2, N, lane);
+            Fr inv2;
+#pragma unroll
+            for (int k = 0; k < 8; k++) inv2.l[k] = kInv2M[k];
+            const Fr c2 = mul(add(sub(v2, add(v1, v1)), v0), inv2);
+            const Fr c1 = sub(sub(v1, v0), c2);
+            cl = add(v0, mul(add(mul(c2, r), c1), r));
+        }
+        Fr x = zero();
+        if (vx) x = ldf(vx, 0, N, lane);
+        Fr p0 = t[0];
+        if (vx) p0 = mul(p0, x);
+        const Fr p1 = sub(cl, p0);
+        if (c == 0) {
+            stf(out, 0, N, lane, p0);
+            stf(out, 1, N, lane, p1);
+            if (dev) {
+                stf(dev, 0, N, lane, p0);
+                stf(dev, 1, N, lane, p1);
+            }
+            return;
+        }
+        Fr p2r = t[tpr];
+        if (vx) p2r = mul(p2r, x);
+        const Fr p1x2 = add(p1, p1);
+        Fr v = add(add(p1x2, p1x2), p1x2);    // 6 p1
+        v = add(v, add(add(p0, p0), p0));     // + 3 p0
+        v = sub(v, add(p2r, p2r));            // - 2 p2raw
+        stf(out, 2, N, lane, v);
+        if (dev) stf(dev, 2, N, lane, v);
     }
 };
 
@@ -403,6 +468,11 @@ __device__ __forceinline__ void accum(Fr (&acc)[3], const Fr& f0, const Fr& f1, 
     acc[0] = add(acc[0], mul(f0, h0));
     acc[1] = add(acc[1], mul(f1, h1));
     acc[2] = add(acc[2], mul(add(f0, f1), add(h0, h1)));
+}
+// p0 and p2raw only (the round's p1 comes from its claim: ClaimFinBn)
+__device__ __forceinline__ void accum(Fr (&acc)[2], const Fr& f0, const Fr& f1, const Fr& h0, const Fr& h1) {
+    acc[0] = add(acc[0], mul(f0, h0));
+    acc[1] = add(acc[1], mul(add(f0, f1), add(h0, h1)));
 }
 
 // ---------------------------------------------------------------- kernels
@@ -600,9 +670,9 @@ __global__ void k_weights(uint64_t I, uint64_t Gm, const Fr* __restrict__ eqc, c
 __global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ v, uint64_t I,
                                                    const uint32_t* __restrict__ mx_off, const uint4* __restrict__ mx_g,
                                                    const Fr* __restrict__ a, const Fr* __restrict__ w, uint32_t* hg,
-                                                   GeoBn g, RedBn red, uint32_t* evals_out) {
+                                                   GeoBn g, RedBn red, const uint32_t* claim, uint32_t* evals_out) {
     const Tile t = tile(g);
-    Fr acc[3] = {zero(), zero(), zero()};
+    Fr acc[2] = {zero(), zero()};  // p0, p2raw
     if (t.active) {
         for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < (I >> 1); i += (uint64_t)gridDim.x * g.rps) {
             Fr h0, h1;
@@ -621,7 +691,7 @@ __global__ void __launch_bounds__(256) k_hg_round0(const uint32_t* __restrict__ 
             accum(acc, ldf(v, 2 * i, g.N, t.q), ldf(v, 2 * i + 1, g.N, t.q), h0, h1);
         }
     }
-    reduce_bn<3>(acc, g, t.active, red, RoundFinBn{evals_out, nullptr, g.N});
+    reduce_bn<2>(acc, g, t.active, red, ClaimFinBn{evals_out, red.evals_dev, claim, nullptr, nullptr, zero(), g.N});
 }
 
 template <bool LANE_HG, bool FOLD>
@@ -631,7 +701,11 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrsBn p, uint64_t npairs, c
     Fr r;
 #pragma unroll
     for (int k = 0; k < 8; k++) r.l[k] = p.r[k];
-    Fr acc[3] = {zero(), zero(), zero()};
+    // fold rounds sum p0 and p2raw (p1 from the claim), phase two's round 0 all three
+    constexpr int C = FOLD ? 2 : 3;
+    Fr acc[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) acc[c] = zero();
     const Fr* hs = reinterpret_cast<const Fr*>(p.hsrc);
     Fr* hd = reinterpret_cast<Fr*>(p.hdst);
     // Phase two folds the lane-independent scalar table: with a power-of-two row tile of at
@@ -688,7 +762,11 @@ __global__ void __launch_bounds__(256) k_round(RoundPtrsBn p, uint64_t npairs, c
         }
         if (valid) accum(acc, f0, f1, h0, h1);
     }
-    reduce_bn<3>(acc, g, t.active, red, RoundFinBn{evals_out, LANE_HG ? nullptr : vx, g.N});
+    if constexpr (FOLD)
+        reduce_bn<2>(acc, g, t.active, red,
+                     ClaimFinBn{evals_out, red.evals_dev, nullptr, red.evals_prev, LANE_HG ? nullptr : vx, r, g.N});
+    else
+        reduce_bn<3>(acc, g, t.active, red, RoundFinBn{evals_out, LANE_HG ? nullptr : vx, g.N, red.evals_dev});
 }
 
 __global__ void k_s_build(uint64_t I, const uint32_t* __restrict__ my_off, const uint4* __restrict__ my_g,
@@ -776,9 +854,11 @@ cudaError_t launch_weights(uint64_t I, uint64_t Gm, const Fr* eqc, const uint4* 
 }
 
 cudaError_t launch_hg_round0(const uint32_t* v, uint64_t I, const uint32_t* mx_off, const uint4* mx_g, const Fr* a,
-                             const Fr* w, uint32_t* hg, const GeoBn& g, uint32_t ctas, RedBn red, uint32_t* evals_out,
-                             cudaStream_t s) {
-    k_hg_round0<<<grid_rows(g, I / 2, ctas), 256, 3 * 8 * 256 * 4, s>>>(v, I, mx_off, mx_g, a, w, hg, g, red, evals_out);
+                             const Fr* w, uint32_t* hg, const GeoBn& g, uint32_t ctas, RedBn red, const uint32_t* claim,
+                             uint32_t* evals_out, cudaStream_t s) {
+    if (!claim) return cudaErrorInvalidValue;
+    k_hg_round0<<<grid_rows(g, I / 2, ctas), 256, 3 * 8 * 256 * 4, s>>>(v, I, mx_off, mx_g, a, w, hg, g, red, claim,
+                                                                       evals_out);
     return cudaGetLastError();
 }
 
@@ -786,6 +866,7 @@ cudaError_t launch_round(bool lane_hg, bool fold_, const RoundPtrsBn& p, uint64_
                          const GeoBn& g, uint32_t ctas, RedBn red, uint32_t* evals_out, cudaStream_t s) {
     const dim3 grid = grid_rows(g, npairs, ctas);
     const size_t smem = 3 * 8 * 256 * 4;
+    if (fold_ && (!red.evals_prev || red.evals_prev == red.evals_dev)) return cudaErrorInvalidValue;
     if (lane_hg && fold_) k_round<true, true><<<grid, 256, smem, s>>>(p, npairs, vx, g, red, evals_out);
     else if (!lane_hg && fold_) k_round<false, true><<<grid, 256, smem, s>>>(p, npairs, vx, g, red, evals_out);
     else if (!lane_hg && !fold_) k_round<false, false><<<grid, 256, smem, s>>>(p, npairs, vx, g, red, evals_out);

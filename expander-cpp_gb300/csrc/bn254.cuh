@@ -32,6 +32,11 @@ struct RedBn {
     unsigned long long* acc;  // comps x N x 8
     unsigned int* ticket;
     unsigned int* done = nullptr;
+    // Device copies of the published round evaluations (3 x N x 8 words each, canonical):
+    // the round kernels write theirs to evals_dev, and a round that takes p1 from its claim
+    // reads the previous round's from evals_prev (a different buffer).
+    const uint32_t* evals_prev = nullptr;
+    uint32_t* evals_dev = nullptr;
 };
 
 struct EqArgsBn {
@@ -66,9 +71,15 @@ cudaError_t launch_eq(Fr* out, const EqArgsBn& a, cudaStream_t s);
 cudaError_t launch_weights(uint64_t I, uint64_t Gm, const Fr* eqc, const uint4* mx_g, const Fr* mx_c,
                            const uint32_t* ax_off, const uint2* ax_g, const Fr* ax_c, Fr* a_out, Fr* w_out,
                            cudaStream_t s);
+// Phase-one hg table and round 0: `claim` (N x 8 words, canonical, device-readable,
+// required) is alpha v(rz1) + beta v(rz2) per copy; the evaluations at 1 are the claim less
+// those at 0.
 cudaError_t launch_hg_round0(const uint32_t* v, uint64_t I, const uint32_t* mx_off, const uint4* mx_g, const Fr* a,
-                             const Fr* w, uint32_t* hg, const GeoBn& g, uint32_t ctas, RedBn red, uint32_t* evals_out,
-                             cudaStream_t s);
+                             const Fr* w, uint32_t* hg, const GeoBn& g, uint32_t ctas, RedBn red, const uint32_t* claim,
+                             uint32_t* evals_out, cudaStream_t s);
+// A sumcheck round.  With fold (every round after a phase's first) the round's claim is the
+// previous round's polynomial at p.r, from red.evals_prev (required), and the evaluations at
+// 1 are that claim less those at 0; phase two's round 0 (no fold) sums all three.
 cudaError_t launch_round(bool lane_hg, bool fold, const RoundPtrsBn& p, uint64_t npairs, const uint32_t* vx,
                          const GeoBn& g, uint32_t ctas, RedBn red, uint32_t* evals_out, cudaStream_t s);
 cudaError_t launch_s_build(uint64_t I, const uint32_t* my_off, const uint4* my_g, const Fr* my_c, const Fr* eqc,

@@ -23,6 +23,7 @@ struct BnWorkspace {
     uint32_t *hg0 = nullptr, *hgA = nullptr, *fA = nullptr, *fB = nullptr;
     bn::Fr *sb[2] = {}, *eqc = nullptr, *eqrx = nullptr, *a = nullptr, *w = nullptr;
     uint32_t *vx = nullptr, *cv = nullptr;
+    uint32_t* ev_dev[2] = {};  // device copies of the round evaluations (round k writes ev_dev[k & 1])
     unsigned long long* acc = nullptr;
     unsigned int* ticket = nullptr;
     unsigned int* flag = nullptr;
@@ -55,6 +56,8 @@ struct BnWorkspace {
         eqc = (bn::Fr*)take(maxO * 32);
         vx = (uint32_t*)take(rowb);
         cv = (uint32_t*)take(rowb);
+        ev_dev[0] = (uint32_t*)take(3 * rowb);
+        ev_dev[1] = (uint32_t*)take(3 * rowb);
         zero_off = o;
         acc = (unsigned long long*)take(3ull * N * 8 * 8);
         ticket = (unsigned int*)take(4096);
@@ -80,6 +83,9 @@ struct BnProver {
     BnWorkspace ws;
     char* block = nullptr;
     std::vector<uint32_t*> vals;  // vals[l]: input of layer l; vals[L]: output of the last layer
+    // the layer's sum is alpha cv1 + beta cv2 (canonical, N x 8 words each): the claimed
+    // values and zero for the output layer, then the previous layer's vx and vy
+    std::vector<uint32_t> cv1, cv2;
 
     BnProver(gkrgpu_ctx& ctx, Lane& lane, const gkrgpu_circuit& circ, uint32_t n) : X(ctx), c(lane), C(circ), N(n) {
         for (int k = 0; k < K_NUM_KERNELS; k++) {
@@ -93,11 +99,16 @@ struct BnProver {
 
     uint64_t rowb() const { return (uint64_t)N * 32; }
     bn::RedBn red() const { return bn::RedBn{ws.acc, ws.ticket}; }
-    bn::RedBn red_mapped() const { return bn::RedBn{ws.acc, ws.ticket, c.done_d()}; }
+    // Round k of a phase publishes to the mapped staging buffer and to ws.ev_dev[k & 1], and
+    // takes its claim from round k - 1's copy.
+    bn::RedBn red_mapped(uint32_t k) const {
+        return bn::RedBn{ws.acc, ws.ticket, c.done_d(), ws.ev_dev[(k + 1) & 1], ws.ev_dev[k & 1]};
+    }
     uint32_t groups(int kid) const { return N / gk[kid].tpr; }
-    // The lane's mapped extra area (words): rows 0..1 of the last table (16N), the claims (8N),
-    // vx in Montgomery form (8N), the input check flag.  Small transfers go through it by
-    // kernels, never queueing on the copy engine behind another proof's bulk copies.
+    // The lane's mapped extra area (words): rows 0..1 of the last table (16N), the claimed
+    // values (8N), vx in Montgomery form (8N), the input check flag, and from word 32N + 64
+    // the claims of phase one's round 0 (8N).  Small transfers go through it by kernels,
+    // never queueing on the copy engine behind another proof's bulk copies.
     uint32_t* mapped(bool dev, uint64_t word) const {
         return reinterpret_cast<uint32_t*>(dev ? c.extra_d() : c.extra_h()) + word;
     }
@@ -120,7 +131,7 @@ struct BnProver {
         block = static_cast<char*>(p);
         ws.plan(block, C, N, sumcheck);
         ck(cudaMemsetAsync(block + ws.zero_off, 0, ws.zero_bytes, c.stream), "cudaMemsetAsync");
-        c.ensure_mapped(3 * rowb(), (32ull * N + 64) * 4);
+        c.ensure_mapped(3 * rowb(), (40ull * N + 64) * 4);
         c.resync_done();
     }
 
@@ -216,13 +227,23 @@ struct BnProver {
 
         // phase one: eqc = alpha eq(rz1) + beta eq(rz2), gate weights, hg + round 0
         eq_table(ws.eqc, rz1, rz2, alpha, beta, m);
+        // round 0's claims, alpha v(rz1) + beta v(rz2) per copy (sumcheck.hpp:129-132)
+        {
+            uint32_t* cl = mapped(false, 32ull * N + 64);
+            for (uint32_t i = 0; i < N; i++)
+                frh::store(frh::add(frh::mul(alpha, frh::load(cv1.data() + 8 * i)),
+                                    frh::mul(beta, frh::load(cv2.data() + 8 * i))),
+                           cl + 8 * i);
+            std::atomic_thread_fence(std::memory_order_seq_cst);
+        }
         c.launch(K_BN_WEIGHTS, 80.0 * Ly.nmul + 72.0 * Ly.nadd + 40.0 * I, [&] {
             return bn::launch_weights(I, Ly.nmul, ws.eqc, Ly.mx_g, Ly.mx_c, Ly.ax_off, Ly.ax_g, Ly.ax_c, ws.a, ws.w,
                                       c.stream);
         });
         c.launch(K_BN_HG_ROUND0, rb * (2.0 * I + Ly.nmul) + 52.0 * Ly.nmul + 36.0 * I, [&] {
             return bn::launch_hg_round0(v, I, Ly.mx_off, Ly.mx_g, ws.a, ws.w, ws.hg0, gk[K_BN_HG_ROUND0],
-                                        ctas[K_BN_HG_ROUND0], red_mapped(), c.evals_d(), c.stream);
+                                        ctas[K_BN_HG_ROUND0], red_mapped(0), mapped(true, 32ull * N + 64),
+                                        c.evals_d(), c.stream);
         });
         fetch(groups(K_BN_HG_ROUND0), n == 1 ? v : nullptr);
         transcript_round(t, rx, 0, n == 1, true, vx_m, vx_c.data());
@@ -240,7 +261,7 @@ struct BnProver {
             const uint64_t npairs = I >> (k + 1);
             c.launch(K_BN_ROUND_LANE, rb * 6.0 * npairs, [&] {
                 return bn::launch_round(true, true, p, npairs, nullptr, gk[K_BN_ROUND_LANE], ctas[K_BN_ROUND_LANE],
-                                        red_mapped(), c.evals_d(), c.stream);
+                                        red_mapped(k), c.evals_d(), c.stream);
             });
             const bool last = (k == n - 1);
             fetch(groups(K_BN_ROUND_LANE), last ? p.fdst : nullptr);
@@ -264,7 +285,7 @@ struct BnProver {
             const uint64_t npairs = I >> 1;
             c.launch(K_BN_ROUND_SCALAR, rb * 2.0 * npairs + 64.0 * npairs, [&] {
                 return bn::launch_round(false, false, p, npairs, ws.vx, gk[K_BN_ROUND_SCALAR], ctas[K_BN_ROUND_SCALAR],
-                                        red_mapped(), c.evals_d(), c.stream);
+                                        red_mapped(0), c.evals_d(), c.stream);
             });
             fetch(groups(K_BN_ROUND_SCALAR), n == 1 ? v : nullptr);
             transcript_round(t, ry, 0, n == 1, false, vy_m.data(), vy_c.data());
@@ -281,7 +302,7 @@ struct BnProver {
             const uint64_t npairs = I >> (k + 1);
             c.launch(K_BN_ROUND_SCALAR, rb * 6.0 * npairs + 192.0 * npairs, [&] {
                 return bn::launch_round(false, true, p, npairs, ws.vx, gk[K_BN_ROUND_SCALAR], ctas[K_BN_ROUND_SCALAR],
-                                        red_mapped(), c.evals_d(), c.stream);
+                                        red_mapped(k), c.evals_d(), c.stream);
             });
             const bool last = (k == n - 1);
             fetch(groups(K_BN_ROUND_SCALAR), last ? p.fdst : nullptr);
@@ -289,6 +310,9 @@ struct BnProver {
             cur_f = p.fdst;
         }
         t.append(vy_c.data(), rowb());
+        // the next layer's sum is alpha vx + beta vy (gkr.hpp:113-119)
+        cv1.swap(vx_c);
+        cv2.swap(vy_c);
     }
 
     void device_front(const uint32_t* h_input, const uint32_t* d_input) {
@@ -317,6 +341,8 @@ struct BnProver {
         c.sync();
         require_canonical();
         memcpy(claimed_v, mapped(false, 16ull * N), rowb());
+        cv1.assign(claimed_v, claimed_v + (size_t)N * 8);
+        cv2.assign((size_t)N * 8, 0u);
 
         for (int li = (int)L - 1; li >= 0; li--) {
             sumcheck_layer(t, (size_t)li, rz1, have_rz2 ? rz2 : nullptr, alpha, beta, rx, ry);
