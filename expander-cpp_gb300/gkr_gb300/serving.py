@@ -15,10 +15,11 @@ admitted in two steps, both by footprint:
 Up to `lanes` proofs run their device stages at once and whatever is pending is taken into
 the lanes as earlier proofs finish, whatever its size.  Requests beyond `max_queue` waiting
 for admission are rejected (admission control), and every result carries its latency.
-Proof buffers come from a pool the server keeps per size: a caller done with a result hands
-its buffer back with Result.release(), so a steady stream of requests writes its proofs into
-memory that is already mapped (a fresh multi-megabyte buffer per request pays first-touch
-page faults, which stall for long when the host is reclaiming or compacting memory).
+Proof buffers come from a pool the server keeps by size class (powers of two from 1 MiB): a
+caller done with a result hands its buffer back with Result.release(), so a steady stream of
+requests, of any mix of sizes, writes its proofs into memory that is already mapped (a fresh
+multi-megabyte buffer per request pays first-touch page faults, which stall for long when the
+host is reclaiming or compacting memory).
 
 The reference has no serving loop (benchmarks/bench_keccak.cpp:32-42 proves in a closed
 loop, one proof per thread).
@@ -76,6 +77,42 @@ class Arena:
         return sum(self.used.values())
 
 
+class BufferPool:
+    """Host buffers for proofs, kept by size class (the next power of two of at least 1 MiB)
+    up to `cap_bytes` in all.  Not thread-safe: the server calls it under its lock."""
+
+    MIN_CLASS = 1 << 20
+
+    def __init__(self, cap_bytes: int):
+        self.cap = cap_bytes
+        self.free = {}  # class size -> [buffers]
+        self.pooled = 0
+
+    @classmethod
+    def size_class(cls, nbytes: int) -> int:
+        c = cls.MIN_CLASS
+        while c < nbytes:
+            c <<= 1
+        return c
+
+    def take(self, nbytes: int):
+        """A pooled buffer of nbytes' class, or None."""
+        c = self.size_class(nbytes)
+        bufs = self.free.get(c)
+        if not bufs:
+            return None
+        self.pooled -= c
+        return bufs.pop()
+
+    def give(self, buf) -> bool:
+        """Keeps `buf` (of a class size) unless the pool is full; returns whether it was kept."""
+        if buf.size != self.size_class(buf.size) or self.pooled + buf.size > self.cap:
+            return False
+        self.free.setdefault(buf.size, []).append(buf)
+        self.pooled += buf.size
+        return True
+
+
 class Result:
     """A finished request: claimed values (R, N), the proof bytes (uint8 array) and times."""
 
@@ -117,7 +154,7 @@ class ProofServer:
     caps the requests in flight."""
 
     def __init__(self, ctx, lanes=16, budget_bytes=150 << 30, arena_bytes=16 << 30, max_queue=1 << 20,
-                 max_admitted=None, pool_bytes=8 << 30):
+                 max_admitted=None, pool_bytes=16 << 30):
         self.ctx = ctx
         self.lanes = lanes
         self.budget = budget_bytes
@@ -135,8 +172,7 @@ class ProofServer:
         self.rejected = 0
         self.completed = 0
         self.stopping = False
-        self.pool = {}  # proof buffers handed back, by size, up to pool_bytes in all
-        self.pool_bytes, self.pooled = pool_bytes, 0
+        self.pool = BufferPool(pool_bytes)  # proof buffers handed back
         self.threads = [threading.Thread(target=self._admit_loop, daemon=True)]
         self.threads += [threading.Thread(target=self._wait_loop, daemon=True) for _ in range(lanes)]
         for t in self.threads:
@@ -186,17 +222,12 @@ class ProofServer:
     # ---------------------------------------------------------------- proof buffers
     def _take(self, size):
         with self.cv:
-            free = self.pool.get(size)
-            if free:
-                self.pooled -= size
-                return free.pop()
-        return np.empty(size, np.uint8)
+            buf = self.pool.take(size)
+        return buf if buf is not None else np.empty(BufferPool.size_class(size), np.uint8)
 
     def _give_back(self, buf):
         with self.cv:
-            if self.pooled + buf.size <= self.pool_bytes:
-                self.pool.setdefault(buf.size, []).append(buf)
-                self.pooled += buf.size
+            self.pool.give(buf)
 
     # ---------------------------------------------------------------- threads
     def _fits(self):

@@ -64,8 +64,9 @@ def test_released_proof_buffers_are_reused(jobs):
         again = srv.submit(dcs[2], wits[2]).result(timeout=60)
         assert again._buf is buf  # the same memory, rewritten
         assert again.proof.tobytes() == alone[2][1]
-        other = srv.submit(dcs[5], wits[5]).result(timeout=60)  # another size: a buffer of its own
+        other = srv.submit(dcs[5], wits[5]).result(timeout=60)  # `again` still holds buf
         assert other.proof.tobytes() == alone[5][1]
+        assert other._buf is not buf
     finally:
         srv.close()
 

@@ -1,8 +1,9 @@
 """Host logic of the serving loop (no GPU): the device arena that holds resident witnesses
-hands out aligned, disjoint ranges, merges freed neighbours and refuses what does not fit."""
+hands out aligned, disjoint ranges, merges freed neighbours and refuses what does not fit;
+the proof-buffer pool reuses buffers across sizes of one class and keeps to its cap."""
 import numpy as np
 
-from gkr_gb300.serving import ALIGN, Arena
+from gkr_gb300.serving import ALIGN, Arena, BufferPool
 
 
 def test_alloc_aligned_disjoint_and_full():
@@ -46,3 +47,21 @@ def test_random_sequence_never_overlaps():
             assert o1 + n1 <= o2
         assert all(o + n <= a.size for o, n in spans)
         assert a.in_use() == sum(live.values())
+
+
+def test_buffer_pool_classes_and_cap():
+    assert BufferPool.size_class(1) == 1 << 20
+    assert BufferPool.size_class((1 << 20) + 1) == 1 << 21
+    assert BufferPool.size_class(3 << 20) == 4 << 20
+    pool = BufferPool(8 << 20)
+    assert pool.take(3 << 20) is None
+    a = np.empty(BufferPool.size_class(3 << 20), np.uint8)
+    assert pool.give(a)
+    assert pool.take((2 << 20) + 1) is a  # another size of the same class
+    assert pool.take(3 << 20) is None
+    b, c = np.empty(4 << 20, np.uint8), np.empty(4 << 20, np.uint8)
+    assert pool.give(b) and pool.give(c)
+    assert not pool.give(np.empty(1 << 20, np.uint8))  # over the cap
+    assert not pool.give(np.empty(3 << 20, np.uint8))  # not a class size
+    assert pool.pooled == 8 << 20
+    assert pool.take(4 << 20) is not None and pool.pooled == 4 << 20
