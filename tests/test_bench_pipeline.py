@@ -98,3 +98,14 @@ def test_a_failed_proof_drains_the_others_before_unwinding():
     # proofs 0..5 were submitted (depth 4 after two waits); every one of them was waited for
     assert sorted(ctx.waited) == list(range(ctx.next_id))
     assert ctx.in_flight == 0
+
+
+def test_reference_formula_bytes_by_hand():
+    """One layer, 4 inputs, 2 outputs, one mul and one add gate, 4 copies of M31, R = 3:
+    (2 + 1 + 2) + (1 + 12) + 16 * 4 + 7 * 4 = 110 vectors, plus the 2 output rows, of 16
+    bytes, and 48 + 24 + 12 * (4 + 8) bytes of gate lists and scalar tables."""
+    import numpy as np
+    from gkr_gb300 import circuit as gc
+    layer = gc.CircuitLayer(1, 2, mul=np.array([[0, 1, 2, 1]], np.uint32), add=np.array([[1, 3, 1]], np.uint32))
+    circ = gc.Circuit([layer])
+    assert bench.reference_formula_bytes(circ, 4) == 112 * 16 + 48 + 24 + 12 * 12
