@@ -1191,11 +1191,18 @@ __global__ void __launch_bounds__(256) k_round_shared(RoundPtrs p, uint64_t npai
 // read once; here each output pair i refolds the eight input rows 8i..8i+7 at r0_j (p.hr[0])
 // and then at r1_j (p.r), stores rows 2i, 2i+1 of f2_j and the folded scalars, and sums the
 // round-2 evaluations (receive_challenge + poly_eval_at, sumcheck_helper.hpp:68-133).  All
-// repetitions in one thread: the eight rows are read once for the R tables.
+// repetitions in one thread: the eight rows are read once for the R tables.  The rows of the
+// next kRowStages - 1 iterations are staged with cp.async while an iteration computes (each
+// thread copies and reads back only its own slots).
+constexpr int kRowStages = 3;
+constexpr int kRowRingSmem = kRowStages * 8 * 16 * 256;
+
 template <int R>
 __global__ void __launch_bounds__(256) k_p2_round2(RoundPtrs p, uint64_t npairs, const uint32_t* __restrict__ vx,
                                                    Geo g, RedScratch red, uint32_t* evals_out) {
+    extern __shared__ uint4 rows8[];  // kRowStages x 8 x blockDim.x
     const TileIdx t = tile_idx(g);
+    const uint32_t B = blockDim.x, tid = threadIdx.x;
     const uint32_t* __restrict__ fs = p.fsrc[0];
     uint32_t acc[2 * R][4];  // 2j: p0, 2j + 1: p2raw
 #pragma unroll
@@ -1203,10 +1210,28 @@ __global__ void __launch_bounds__(256) k_p2_round2(RoundPtrs p, uint64_t npairs,
 #pragma unroll
         for (int l = 0; l < 4; l++) acc[c][l] = 0u;
     if (t.active) {
-        for (uint64_t i = (uint64_t)blockIdx.x * g.rps + t.rs; i < npairs; i += (uint64_t)gridDim.x * g.rps) {
+        const uint64_t step = (uint64_t)gridDim.x * g.rps;
+        const uint64_t i0 = (uint64_t)blockIdx.x * g.rps + t.rs;
+        auto stage = [&](uint64_t i, int slot) {
+            if (i < npairs) {
+                uint4* st = rows8 + (size_t)slot * 8 * B + tid;
+#pragma unroll
+                for (int k = 0; k < 8; k++) cp_async16(st + k * B, fs + (8 * i + k) * g.N + t.lane0);
+            }
+            cp_async_commit();  // one group per iteration, empty past the end
+        };
+#pragma unroll
+        for (int q = 0; q < kRowStages - 1; q++) stage(i0 + q * step, q);
+        int slot = 0;
+        for (uint64_t i = i0; i < npairs; i += step) {
+            // refill the slot read in the previous iteration, then wait for this one
+            stage(i + (kRowStages - 1) * step, slot == 0 ? kRowStages - 1 : slot - 1);
+            cp_async_wait<kRowStages - 1>();
+            const uint4* st = rows8 + (size_t)slot * 8 * B + tid;
             uint4 a[8];
 #pragma unroll
-            for (int k = 0; k < 8; k++) a[k] = ld4(fs, 8 * i + k, g.N, t.lane0);
+            for (int k = 0; k < 8; k++) a[k] = st[k * B];
+            slot = slot + 1 == kRowStages ? 0 : slot + 1;
 #pragma unroll
             for (int j = 0; j < R; j++) {
                 const uint32_t r0 = p.hr[0][j], r1 = p.r[j];
@@ -1234,11 +1259,13 @@ __global__ void __launch_bounds__(256) k_p2_round2(RoundPtrs p, uint64_t npairs,
                 }
             }
         }
+        cp_async_wait<0>();
     }
 #pragma unroll
     for (int c = 0; c < 2 * R; c++)
 #pragma unroll
         for (int l = 0; l < 4; l++) acc[c][l] = m31::from_u32(acc[c][l]);
+    __syncthreads();  // the ring is reused as the reduction's scratch
     reduce_group<2 * R>(acc, g, t.active, red, 0,
                         ClaimFin{red, evals_out, nullptr, {p.r[0], p.r[1], p.r[2]}, g.N, (uint32_t)R, vx});
 }
@@ -1740,6 +1767,21 @@ static size_t hg0_smem(size_t ring_bytes, size_t red_bytes) {
     return ring_bytes > red_bytes ? ring_bytes : red_bytes;
 }
 
+// Dynamic shared memory of a kernel with a row ring (kRowRingSmem at most): the opt-in above
+// 48 KiB is set once per device and kernel (one instance of this function per kernel).
+template <auto Kernel>
+static size_t ring_smem(size_t bytes) {
+    static std::atomic<uint64_t> opted{0};  // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(opted.load(std::memory_order_relaxed) & bit)) {
+        cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kRowRingSmem);
+        opted.fetch_or(bit);
+    }
+    return bytes;
+}
+
 Geo tail_geo(uint32_t N) {
     Geo g;
     g.N = N;
@@ -1930,12 +1972,14 @@ cudaError_t launch_p1_round2(int reps, const RoundPtrs& p, uint64_t npairs, cons
 
 cudaError_t launch_p2_round2(int reps, const RoundPtrs& p, uint64_t npairs, const uint32_t* vx, const Geo& g,
                              uint32_t block, uint32_t ctas, RedScratch red, uint32_t* evals_out, cudaStream_t s) {
-    if (!red.evals_dev) return cudaErrorInvalidValue;
+    if (!red.evals_dev || block > 256) return cudaErrorInvalidValue;
     LaunchShape sh = row_shape(g, npairs, block, ctas, 2 * reps);
+    const size_t ring = (size_t)kRowStages * 8 * sizeof(uint4) * block;
+    const size_t smem = ring > sh.smem ? ring : sh.smem;
     switch (reps) {
-        case 1: k_p2_round2<1><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out); break;
-        case 2: k_p2_round2<2><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out); break;
-        case 3: k_p2_round2<3><<<sh.grid, sh.block, sh.smem, s>>>(p, npairs, vx, g, red, evals_out); break;
+        case 1: k_p2_round2<1><<<sh.grid, sh.block, ring_smem<k_p2_round2<1>>(smem), s>>>(p, npairs, vx, g, red, evals_out); break;
+        case 2: k_p2_round2<2><<<sh.grid, sh.block, ring_smem<k_p2_round2<2>>(smem), s>>>(p, npairs, vx, g, red, evals_out); break;
+        case 3: k_p2_round2<3><<<sh.grid, sh.block, ring_smem<k_p2_round2<3>>(smem), s>>>(p, npairs, vx, g, red, evals_out); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
