@@ -18,16 +18,21 @@
 /* ---------------------------------------------------------------- M31 field
  * include/field/M31.hpp:64-93 (scalar) and include/field/M31_avx.tcc:97-176 (packed);
  * both return canonical values in [0, p) for canonical inputs. */
-static inline uint32_t m_add(uint32_t a, uint32_t b) { uint32_t r = a + b; return r >= P ? r - P : r; }
-static inline uint32_t m_neg(uint32_t a) { return a == 0 ? 0 : P - a; }
-static inline uint32_t m_sub(uint32_t a, uint32_t b) { return m_add(a, m_neg(b)); }
+/* Branch-free forms (a conditional subtraction as a minimum of two candidates) so that gcc
+ * vectorises the per-lane loops with portable flags; the values are the same. */
+static inline uint32_t m_umin(uint32_t a, uint32_t b) { return a < b ? a : b; }
+/* a + b < 2^32: r - p wraps above r exactly when r < p */
+static inline uint32_t m_add(uint32_t a, uint32_t b) { uint32_t r = a + b; return m_umin(r, r - P); }
+/* a - b wraps above p exactly when a < b, and then d + p (mod 2^32) is the result */
+static inline uint32_t m_sub(uint32_t a, uint32_t b) { uint32_t d = a - b; return m_umin(d, d + P); }
+/* a b < 2^62: (x & p) + (x >> 31) < 2p for canonical inputs, then one subtraction */
 static inline uint32_t m_mul(uint32_t a, uint32_t b) {
     uint64_t x = (uint64_t)a * b;
-    x = (x & P) + (x >> 31);
-    return (uint32_t)(x >= P ? x - P : x);
+    uint32_t s = ((uint32_t)x & P) + (uint32_t)(x >> 31);
+    return m_umin(s, s - P);
 }
 /* M31::from_bytes / PackedM31::from_bytes: M31.hpp:111-116, M31_avx.tcc:62-67 */
-static inline uint32_t m_reduce(uint32_t x) { x = (x & P) + (x >> 31); return x >= P ? x - P : x; }
+static inline uint32_t m_reduce(uint32_t x) { x = (x & P) + (x >> 31); return m_umin(x, x - P); }
 
 /* ---------------------------------------------------------------- SHA-256 (FIPS 180-4)
  * The reference hashes with Bitcoin Core's CSHA256 (lib/btc_sha256/crypto/sha256.cpp),
