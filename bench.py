@@ -265,7 +265,7 @@ def cpu_sample(circ, args, n_steps=1, warmup=0):
 # The oracle port against the compiled reference (VectorizedM31, AVX-512) on the same
 # 8-copy proof of this circuit, one thread each, measured on an x86-64 host where both
 # build; the Arm GPU host has no reference tree, so there the port stands in for it.
-PORT_VS_REFERENCE = {"port_s": 10.0, "reference_s": 6.2, "ratio": 1.6,
+PORT_VS_REFERENCE = {"port_s": 8.9, "reference_s": 6.1, "ratio": 1.45,
                      "note": "single-thread 8-copy config-2 proof on a Xeon with AVX-512; the port understates the "
                              "reference's CPU speed by about this factor"}
 

@@ -19,7 +19,9 @@
  * include/field/M31.hpp:64-93 (scalar) and include/field/M31_avx.tcc:97-176 (packed);
  * both return canonical values in [0, p) for canonical inputs. */
 /* Branch-free forms (a conditional subtraction as a minimum of two candidates) so that gcc
- * vectorises the per-lane loops with portable flags; the values are the same. */
+ * vectorises the per-lane loops with portable flags; the values are the same.  The hot lane
+ * loops carry `ivdep`: lane k of a row depends only on lane k of its sources (an in-place
+ * fold reads and writes the same lane), so gcc may skip its run-time overlap checks. */
 static inline uint32_t m_umin(uint32_t a, uint32_t b) { return a < b ? a : b; }
 /* a + b < 2^32: r - p wraps above r exactly when r < p */
 static inline uint32_t m_add(uint32_t a, uint32_t b) { uint32_t r = a + b; return m_umin(r, r - P); }
@@ -194,12 +196,14 @@ static void layer_eval(const oracle_layer* L, uint32_t N, const uint32_t* in, ui
         const uint32_t* s = L->mul + 4 * g;
         uint32_t* o = out + (uint64_t)s[0] * N;
         const uint32_t *a = in + (uint64_t)s[1] * N, *b = in + (uint64_t)s[2] * N;
+        #pragma GCC ivdep
         for (uint32_t k = 0; k < N; k++) o[k] = m_add(o[k], m_mul(m_mul(a[k], b[k]), s[3]));
     }
     for (uint64_t g = 0; g < L->n_add; g++) {
         const uint32_t* s = L->add + 3 * g;
         uint32_t* o = out + (uint64_t)s[0] * N;
         const uint32_t* a = in + (uint64_t)s[1] * N;
+        #pragma GCC ivdep
         for (uint32_t k = 0; k < N; k++) o[k] = m_add(o[k], m_mul(a[k], s[2]));
     }
 }
@@ -239,6 +243,7 @@ void oracle_eval_multilinear(const uint32_t* evals, uint32_t nb_vars, uint32_t N
     for (uint32_t v = 0; v < nb_vars; v++) {
         for (uint64_t i = 0; i < cur; i++) {
             uint32_t *d = s + i * N, *a = s + 2 * i * N, *b = s + (2 * i + 1) * N;
+            #pragma GCC ivdep
             for (uint32_t k = 0; k < N; k++) d[k] = m_add(a[k], m_mul(m_sub(b[k], a[k]), r[v]));
         }
         cur >>= 1;
@@ -294,6 +299,7 @@ static void ph_poly_eval_at(const prod_helper* h, uint32_t var_idx, const uint8_
     for (uint64_t i = 0; i < n; i++) {
         if (!gate_exists[2 * i] && !gate_exists[2 * i + 1]) continue;
         const uint32_t *f0 = src + 2 * i * N, *f1 = f0 + N, *g0 = h->bk_hg + 2 * i * N, *g1 = g0 + N;
+        #pragma GCC ivdep
         for (uint32_t k = 0; k < N; k++) {
             p0[k] = m_add(p0[k], m_mul(f0[k], g0[k]));
             p1[k] = m_add(p1[k], m_mul(f1[k], g1[k]));
@@ -314,10 +320,12 @@ static void ph_receive_challenge(prod_helper* h, uint32_t r, uint8_t* gate_exist
         const uint32_t *ga = h->bk_hg + 2 * i * N, *gb = ga + N;
         if (!gate_exists[2 * i] && !gate_exists[2 * i + 1]) {
             gate_exists[i] = 0;
+            #pragma GCC ivdep
             for (uint32_t k = 0; k < N; k++) f[k] = m_add(a[k], m_mul(m_sub(b[k], a[k]), r));
             memset(g, 0, N * 4);
         } else {
             gate_exists[i] = 1;
+            #pragma GCC ivdep
             for (uint32_t k = 0; k < N; k++) {
                 f[k] = m_add(a[k], m_mul(m_sub(b[k], a[k]), r));
                 g[k] = m_add(ga[k], m_mul(m_sub(gb[k], ga[k]), r));
@@ -358,6 +366,7 @@ static void prepare_g_x(gkr_helper* h) {
         uint32_t w = m_mul(s[3], pad->eq_rz1[z]);
         uint32_t* hg = pad->hg_evals + (uint64_t)x * N;
         const uint32_t* vy = h->layer_input + (uint64_t)y * N;
+        #pragma GCC ivdep
         for (uint32_t k = 0; k < N; k++) hg[k] = m_add(hg[k], m_mul(vy[k], w));
         pad->gate_exists[x] = 1;
     }
@@ -366,6 +375,7 @@ static void prepare_g_x(gkr_helper* h) {
         uint32_t x = s[1], z = s[0];
         uint32_t w = m_mul(s[2], pad->eq_rz1[z]);
         uint32_t* hg = pad->hg_evals + (uint64_t)x * N;
+        #pragma GCC ivdep
         for (uint32_t k = 0; k < N; k++) hg[k] = m_add(hg[k], w);
         pad->gate_exists[x] = 1;
     }
@@ -385,6 +395,7 @@ static void prepare_h_y(gkr_helper* h, const uint32_t* v_rx) {
         uint32_t x = s[1], y = s[2], z = s[0];
         uint32_t w = m_mul(m_mul(pad->eq_rz1[z], pad->eq_rx[x]), s[3]);
         uint32_t* hg = pad->hg_evals + (uint64_t)y * N;
+        #pragma GCC ivdep
         for (uint32_t k = 0; k < N; k++) hg[k] = m_add(hg[k], m_mul(v_rx[k], w));
         pad->gate_exists[y] = 1;
     }
